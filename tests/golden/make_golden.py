@@ -1,0 +1,41 @@
+"""Regenerate the golden fixtures in this directory from the reference checkout.
+
+Run from the repository root in a container that has the reference mounted:
+    python tests/golden/make_golden.py /path/to/pocketwind
+
+cube_binary.json: the 12 facets of tests/fixtures/stl/cube-binary.stl, read the
+way src/geometry/stl.ts:29-41 reads a binary STL (skip the 80-byte header and
+4-byte count; per 50-byte record skip the normal, take nine little-endian
+float32 coordinates).  tests/unit/voxelize/fixtures.ts:5-20 scales this unit
+cube into the boxes the voxelizer tests use.
+"""
+import json
+import struct
+import sys
+from pathlib import Path
+
+
+def read_binary_stl(path: Path):
+    data = path.read_bytes()
+    (count,) = struct.unpack_from("<I", data, 80)
+    out = []
+    for t in range(count):
+        start = 84 + 50 * t + 12
+        out.extend(struct.unpack_from("<9f", data, start))
+    return count, out
+
+
+def main():
+    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    count, positions = read_binary_stl(ref / "tests/fixtures/stl/cube-binary.stl")
+    here = Path(__file__).resolve().parent
+    (here / "cube_binary.json").write_text(json.dumps({
+        "source": "tests/fixtures/stl/cube-binary.stl",
+        "triangle_count": count,
+        "positions": positions,
+    }, indent=1) + "\n")
+    print("wrote cube_binary.json with", count, "triangles")
+
+
+if __name__ == "__main__":
+    main()
