@@ -1,0 +1,278 @@
+#!/usr/bin/env python3
+"""Benchmark of the fused D3Q19 stream-collide on one GB300.
+
+Workload: the bluff vehicle body scaled x4 into a 512 x 256 x 256 tunnel
+(33,554,432 cells), regularized collision with Smagorinsky LES (C_s = 0.1) and the
+Werner-Wengle wall model, floor on, u = 0.05, nu = 0.025 (Re 320 on the 160-cell
+body), populations stored in FP16 (x 2^15, hash-dithered) -- the
+headline -- with FP32 and BF16 storage measured in the same run.  A step is one
+lattice update of every cell; the 2.5 GB (FP16) / 5.1 GB (FP32) population array
+is far larger than the 129 MB L2, so no flush is needed between steps.
+
+value   = MLUPS (million lattice-cell updates per second) of the FP16 kernel with
+          state resident in HBM, timed with CUDA events on the solver's stream.
+e2e     = the same metric through the public solver API the reference's headless
+          runner uses (src/app/case-run.ts:154-169): host mesh -> GPU voxelizer ->
+          create -> {step 8, encode force, read force} loop, wall clock, with the
+          mesh upload (once) and every force readback inside the timed region.
+roofline: algorithmic bytes per cell update B = 2 * 19 * s + 1/8 (s = 2 bytes),
+          achieved = cells * B / mean kernel time, peak = measured HBM copy GB/s.
+cpu_baseline: the binary64 restatement of the reference's CpuSolver (the
+          reference's CPU path; the TypeScript original cannot run here), on all
+          host cores, over a bounded number of full-domain steps.
+
+--impl reference runs only that CPU path and prints its own line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NX, NY, NZ = 512, 256, 256
+SCALE = 4.0
+U_IN = 0.05
+NU = U_IN * 40 * SCALE / 320  # Re 320 on the body length (40 * SCALE cells)
+TAU0 = 0.5 + 3 * NU
+METRIC = "D3Q19 MLUPS & % HBM roofline, FP16-store vs FP32, drag err vs FP64 at 1 GB300"
+BYTES = {"f32": 2 * 19 * 4 + 0.125, "f16": 2 * 19 * 2 + 0.125, "bf16": 2 * 19 * 2 + 0.125}
+
+
+def read_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def read_traffic():
+    """Per-launch DRAM bytes of the FP16 step kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "stream_collide_traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if not self.proc:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.file.flush()
+        self.file.seek(0)
+        rows = [r.split(",") for r in self.file.read().strip().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for k, name in enumerate(names):
+                    if r[5 + k].strip().lower().startswith("active"):
+                        reasons.add(name)
+            except (ValueError, IndexError):
+                continue
+        if sm:
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                   "samples": len(sm)}
+        return out
+
+
+def build_case():
+    from pocketwind_gb300 import meshes
+    return meshes.vehicle_case_mesh(NX, NY, SCALE)
+
+
+def run_ours(args, rank, world):
+    import numpy as np
+    from pocketwind_gb300 import _lib
+    from pocketwind_gb300.geometry import voxelize
+    from pocketwind_gb300.solver import GpuSolver, SolverParams
+
+    _lib.require_gpu()
+    body = build_case()
+    grid = voxelize(body, None, (NX, NY, NZ), True)
+    cells = NX * NY * NZ
+    results = {}
+    for precision in ("f16", "f32", "bf16"):
+        solver = GpuSolver.create((NX, NY, NZ), grid, SolverParams(tau0=TAU0, u_in=U_IN, les=True, operator="reg",
+                                                                   precision=precision))
+        if isinstance(solver, Exception):
+            raise solver
+        solver.step(args.warmup)
+        solver.time_steps(0)
+        clocks = None
+        if precision == "f16":
+            sampler = ClockSampler()
+            sampler.start()
+        ms = solver.time_steps(args.steps)
+        if precision == "f16":
+            clocks = sampler.stop()
+        unstable = False
+        solver.step(1, True)
+        unstable = solver.guard_unstable()
+        results[precision] = {"ms": ms, "clocks": clocks, "unstable": unstable}
+        solver.destroy()
+    # end-to-end through the public API (wall clock): mesh upload + voxelize + create + sampled stepping
+    import time as _t
+    t0 = _t.perf_counter()
+    grid2 = voxelize(body, None, (NX, NY, NZ), True)
+    solver = GpuSolver.create((NX, NY, NZ), grid2, SolverParams(tau0=TAU0, u_in=U_IN, les=True, operator="reg",
+                                                                precision="f16"))
+    samples = max(1, args.steps // 8)
+    for _ in range(samples):
+        solver.step(8)
+        solver.encode_force()
+        f = solver.read_force()
+    e2e_s = _t.perf_counter() - t0
+    solver.destroy()
+    e2e_steps = samples * 8
+    return results, e2e_s, e2e_steps, body.positions.nbytes, cells, grid
+
+
+def cpu_baseline(grid_flags, steps, threads):
+    """Binary64 CpuSolver restatement on the host cores over `steps` full-domain steps."""
+    from oracle import oracle as O
+    s = O.Cpu64((NX, NY, NZ), TAU0, operator="reg", les=True, flags=grid_flags,
+                equilibrium_state=(1.0, (U_IN, 0.0, 0.0)), threads=threads)
+    t0 = time.perf_counter()
+    s.step(steps)
+    dt = time.perf_counter() - t0
+    return NX * NY * NZ * steps / dt / 1e6, dt
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    threads = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from pocketwind_gb300 import meshes
+        from oracle import oracle as O
+        body = build_case()
+        g = O.voxelize(body.positions, None, (NX, NY, NZ), True, link_fractions=False)
+        flags = g.geometry[: NX * NY * NZ]
+        per = []
+        cpu_steps = max(1, min(args.steps, args.cpu_steps))
+        mlups, dt = cpu_baseline(flags, cpu_steps, threads)
+        line = {"metric": METRIC, "value": round(mlups, 3), "unit": "MLUPS", "n_gpus": args.gpus,
+                "steps": cpu_steps, "warmup": 0, "ms_per_step": round(1000 * dt / cpu_steps, 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "impl": "reference",
+                "config": {"workload": "vehicle body x4, 512x256x256, REG+LES+wall model, floor", "cells": NX * NY * NZ},
+                "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
+                                 "sample": f"{cpu_steps} full-domain steps of the binary64 CpuSolver restatement"},
+                "e2e": {"value": round(mlups, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    results, e2e_s, e2e_steps, mesh_bytes, cells, grid = run_ours(args, rank, world)
+    ms = results["f16"]["ms"]
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    if rank != 0:
+        return
+    peak, peak_kind = read_peaks()
+    mlups = cells * args.steps * world / (ms * 1e3)
+    achieved = cells * BYTES["f16"] / (ms / args.steps / 1e3) / 1e9
+    traffic = read_traffic()
+    line = {
+        "metric": METRIC,
+        "value": round(mlups, 2),
+        "unit": "MLUPS",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms / args.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 arithmetic, f16 storage",
+        "data": "synthetic (parametric bluff-body mesh)",
+        "config": {"workload": "vehicle body x4, 512x256x256, REG+LES+wall model, floor, FP16 storage",
+                   "cells": cells, "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (2.5 GB populations)"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                     "bytes_per_cell": BYTES["f16"],
+                     "traffic": traffic.get("bytes_per_launch") if traffic else None},
+        "storage_sweep": {p: {"mlups": round(cells * args.steps / (r["ms"] * 1e3), 2),
+                              "hbm_frac": round(cells * BYTES[p] / (r["ms"] / args.steps / 1e3) / 1e9 / peak, 4),
+                              "stable": not r["unstable"]}
+                          for p, r in results.items()},
+        "e2e": {"value": round(cells * e2e_steps / (e2e_s * 1e6), 2), "unit": "MLUPS",
+                "h2d_bytes_per_step": round(mesh_bytes / e2e_steps, 2),
+                "d2h_bytes_per_step": round(24 / 8, 2)},
+        "gpu_launches": args.steps,
+        "clocks": results["f16"]["clocks"],
+    }
+    line["storage_sweep"]["f16_over_f32"] = round(line["storage_sweep"]["f16"]["mlups"] /
+                                                  line["storage_sweep"]["f32"]["mlups"], 3)
+    if world == 1 and args.cpu_steps > 0:
+        flags = grid.flags.copy()
+        cmlups, cdt = cpu_baseline(flags, args.cpu_steps, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": round(cmlups, 3), "unit": "MLUPS", "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"{args.cpu_steps} full-domain steps of the binary64 CpuSolver "
+                                          f"restatement ({cdt:.1f} s)"}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,115 @@
+// Shared device definitions of the D3Q19 solver: lattice tables, storage codecs,
+// kernel parameter blocks.  Lattice order and weights follow
+// src/lbm/lattice.ts:1-52 and src/lbm/shaders/common.wgsl:1-22 of the reference.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace pw {
+
+enum : uint32_t { FLUID = 0, SOLID = 1, SUPPORT = 2, FLOOR = 3, EQ = 4 };
+enum : int { STORE_F32 = 0, STORE_F16 = 1, STORE_BF16 = 2 };
+enum : int { OP_TRT = 0, OP_REG = 1 };
+
+// Direction i: velocity (CX, CY, CZ); opposite pairs are (1,2), (3,4), ...
+__host__ __device__ constexpr int cx_of(int i) {
+  return i == 1 || i == 7 || i == 9 || i == 13 || i == 15 ? 1
+         : (i == 2 || i == 8 || i == 10 || i == 14 || i == 16 ? -1 : 0);
+}
+__host__ __device__ constexpr int cy_of(int i) {
+  return i == 3 || i == 7 || i == 11 || i == 14 || i == 17 ? 1
+         : (i == 4 || i == 8 || i == 12 || i == 13 || i == 18 ? -1 : 0);
+}
+__host__ __device__ constexpr int cz_of(int i) {
+  return i == 5 || i == 9 || i == 11 || i == 16 || i == 18 ? 1
+         : (i == 6 || i == 10 || i == 12 || i == 15 || i == 17 ? -1 : 0);
+}
+__host__ __device__ constexpr int opp_of(int i) { return i == 0 ? 0 : ((i & 1) ? i + 1 : i - 1); }
+// binary32 weights, each 1/3, 1/18 or 1/36 rounded once (WGSL const-expression).
+__host__ __device__ constexpr float w_of(int i) {
+  return i == 0 ? 0.333333343267440796f : (i < 7 ? 0.0555555559694766998f : 0.0277777779847383499f);
+}
+
+__device__ __forceinline__ bool is_wall_kind(uint32_t k) { return k >= SOLID && k <= FLOOR; }
+
+// ------------------------------------------------------------ storage codecs
+// lowbias32 dithering of the discarded bits (src/lbm/shaders/prelude-f16.wgsl:7-22).
+__device__ __forceinline__ uint32_t lowbias32(uint32_t bits, uint32_t i, uint32_t n) {
+  uint32_t r = bits ^ (n * 0x9e3779b9u) ^ (i * 0x85ebca6bu);
+  r = (r ^ (r >> 16)) * 0x7feb352du;
+  r = (r ^ (r >> 15)) * 0x846ca68bu;
+  r ^= r >> 16;
+  return r;
+}
+
+template <int S> struct Store;
+
+template <> struct Store<STORE_F32> {
+  using T = float;
+  static constexpr float kScale = 1.0f;
+  static constexpr float kInvScale = 1.0f;
+  __device__ __forceinline__ static float decode(float v) { return v; }
+  __device__ __forceinline__ static float encode(float v, uint32_t, uint32_t) { return v; }
+  __device__ __forceinline__ static float nan_code() { return __int_as_float(0x7fc00000); }
+};
+
+template <> struct Store<STORE_F16> {
+  using T = __half;
+  static constexpr float kScale = 32768.0f;
+  static constexpr float kInvScale = 1.0f / 32768.0f;
+  // Division by a power of two is exact, so this equals f32(h) / 2^15.
+  __device__ __forceinline__ static float decode(__half h) { return __half2float(h) * kInvScale; }
+  __device__ __forceinline__ static __half encode(float value, uint32_t i, uint32_t n) {
+    float scaled = value * kScale;
+    uint32_t bits = __float_as_uint(scaled);
+    uint32_t magnitude = bits & 0x7fffffffu;
+    if (magnitude < 0x38800000u) return __float2half_rn(scaled);
+    uint32_t random = lowbias32(bits, i, n);
+    uint32_t increment = ((random & 0x1fffu) < (magnitude & 0x1fffu)) ? 0x2000u : 0u;
+    uint32_t rounded = (magnitude & 0xffffe000u) + increment;
+    return __float2half_rn(__uint_as_float((bits & 0x80000000u) | rounded));
+  }
+};
+
+template <> struct Store<STORE_BF16> {
+  using T = __nv_bfloat16;
+  static constexpr float kScale = 1.0f;
+  static constexpr float kInvScale = 1.0f;
+  __device__ __forceinline__ static float decode(__nv_bfloat16 h) { return __bfloat162float(h); }
+  // The f16 dithering rule applied to the 16 bits bfloat16 discards.
+  __device__ __forceinline__ static __nv_bfloat16 encode(float value, uint32_t i, uint32_t n) {
+    uint32_t bits = __float_as_uint(value);
+    uint32_t magnitude = bits & 0x7fffffffu;
+    if (magnitude < 0x00800000u || magnitude >= 0x7f800000u) return __float2bfloat16_rn(value);
+    uint32_t random = lowbias32(bits, i, n);
+    uint32_t increment = ((random & 0xffffu) < (magnitude & 0xffffu)) ? 0x10000u : 0u;
+    uint32_t rounded = (magnitude & 0xffff0000u) + increment;
+    return __ushort_as_bfloat16((unsigned short)(((bits & 0x80000000u) | rounded) >> 16));
+  }
+};
+
+// Step kernels run blocks of one warp along x by kBlockY rows.
+constexpr int kBlockX = 32;
+constexpr int kBlockY = 4;
+
+// ------------------------------------------------------------ parameter blocks
+struct StepParams {
+  void *f;                 // 19 * stride population codes (AA layout)
+  float4 *macros;          // (rho, ux, uy, uz) per cell
+  const float4 *plane_in;  // outlet upstream velocity written by the previous step
+  float4 *plane_out;       // this step's upstream velocity
+  const uint32_t *flags;   // packed flags (kind | wall bits << 3)
+  const uint32_t *special; // bit per cell: anything but plain fluid without wall links
+  double *partials;        // 3 doubles per block: momentum exchange of this step's output
+  uint32_t *status;        // bit 0: density guard tripped on a macro step
+  uint32_t nx, ny, nz;
+  uint32_t stride;         // elements between direction planes
+  float u_in;              // inlet speed of this step
+  float nu, cs_term, lambda;
+  float tau0, omega_plus, omega_minus;  // binary32 constants of the LES-free operator
+  int write_macro;
+};
+
+}  // namespace pw

@@ -1,0 +1,500 @@
+// Solver domain: the C-ABI counterpart of the reference's GpuSolver and GpuForce
+// (src/lbm/gpu-solver.ts:135-465, src/lbm/gpu-force.ts:45-216).
+//
+// Memory (one GB300, everything resident in HBM):
+//   f         19 * stride population codes, updated in place (AA pattern)
+//   macros    float4 per cell
+//   plane[2]  float4 per (y, z): outlet upstream velocity, double-buffered by step parity
+//   flags     u32 per cell; special: 1 bit per cell (non-plain cells)
+//   partials[2] 3 doubles per step block: momentum exchange of the even / odd states
+// Stepping queues one fused kernel per step on the domain's stream; runs of
+// steps without ramping are replayed from captured CUDA graphs.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <tuple>
+
+#include "pw_internal.h"
+
+#include "pw_launch.h"
+
+using namespace pwhost;
+
+namespace {
+
+constexpr int kGraphChunk = 64;  // steps per captured graph
+
+__global__ void special_kernel(const uint32_t *flags, size_t cells, uint32_t *special) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t bit = 0;
+  if (i < cells) {
+    uint32_t f = flags[i];
+    bit = (f & 7u) != pw::FLUID || (f >> 3) != 0u;
+  }
+  uint32_t word = __ballot_sync(0xffffffffu, bit);
+  if ((threadIdx.x & 31) == 0 && i < cells) special[i >> 5] = word;
+}
+
+__global__ void first_fluid_kernel(const uint32_t *flags, size_t cells, unsigned long long *out) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < cells && (flags[i] & 7u) == pw::FLUID) atomicMin(out, (unsigned long long)i);
+}
+
+// Sum both parities' partials: 0.5 * (F(even state) + F(odd state)) (force.wgsl:31-32,
+// reduce.wgsl), binary64, fixed order.
+__global__ void force_reduce_kernel(const double *a, const double *b, size_t nblocks, double *out) {
+  __shared__ double sh[256][3];
+  double s0 = 0, s1 = 0, s2 = 0;
+  for (size_t k = threadIdx.x; k < nblocks; k += 256) {
+    s0 += a[3 * k] + b[3 * k];
+    s1 += a[3 * k + 1] + b[3 * k + 1];
+    s2 += a[3 * k + 2] + b[3 * k + 2];
+  }
+  sh[threadIdx.x][0] = s0; sh[threadIdx.x][1] = s1; sh[threadIdx.x][2] = s2;
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if (threadIdx.x < (unsigned)st)
+      for (int c = 0; c < 3; c++) sh[threadIdx.x][c] += sh[threadIdx.x + st][c];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int c = 0; c < 3; c++) out[c] = 0.5 * sh[0][c];
+}
+
+enum ForceState { FORCE_IDLE = 0, FORCE_ENCODED = 1 };
+
+}  // namespace
+
+struct pw_domain {
+  pw_domain_desc desc{};
+  uint32_t nx = 0, ny = 0, nz = 0;
+  size_t cells = 0;
+  uint32_t stride = 0;
+  size_t esize = 4;
+  void *f = nullptr;
+  float4 *macros = nullptr;
+  float4 *plane[2] = {nullptr, nullptr};
+  uint32_t *flags = nullptr, *special = nullptr;
+  double *partials[2] = {nullptr, nullptr};
+  size_t nblocks = 0;
+  double *force_dev = nullptr;
+  double *force_host = nullptr;   // pinned staging slot
+  uint32_t *status_dev = nullptr;
+  uint32_t *status_host = nullptr;
+  double *totals_dev = nullptr;
+  void *scratch = nullptr;        // readout / write-in buffer, allocated on first use
+  uint64_t first_fluid = ~0ull;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t force_event = nullptr;
+  uint64_t steps = 0;
+  int force_state = FORCE_IDLE;
+  uint64_t force_step = 0;
+  float u_in = 0, nu = 0, cs_term = 0, lambda = 0, tau0 = 0, om_p = 0, om_m = 0;
+  dim3 grid;
+  // captured step runs: key (start parity, write macro on last) -> graph of kGraphChunk steps
+  std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
+};
+
+namespace pwhost {
+void domain_dims(const pw_domain *d, uint32_t *nx, uint32_t *ny, uint32_t *nz) {
+  *nx = d->nx; *ny = d->ny; *nz = d->nz;
+}
+}  // namespace pwhost
+
+namespace {
+
+pw::StepParams params_for(const pw_domain *d, uint64_t step, float u_in, int write_macro) {
+  pw::StepParams p{};
+  int par = (int)(step & 1);
+  p.f = d->f;
+  p.macros = d->macros;
+  p.plane_in = d->plane[par ^ 1];
+  p.plane_out = d->plane[par];
+  p.flags = d->flags;
+  p.special = d->special;
+  p.partials = d->partials[par];
+  p.status = d->status_dev;
+  p.nx = d->nx; p.ny = d->ny; p.nz = d->nz;
+  p.stride = d->stride;
+  p.u_in = u_in;
+  p.nu = d->nu; p.cs_term = d->cs_term; p.lambda = d->lambda;
+  p.tau0 = d->tau0; p.omega_plus = d->om_p; p.omega_minus = d->om_m;
+  p.write_macro = write_macro;
+  return p;
+}
+
+// Queue step number `step` (1-based) with the given inlet speed.
+void enqueue_step(pw_domain *d, uint64_t step, float u_in, int write_macro) {
+  pw::StepParams p = params_for(d, step, u_in, write_macro);
+  if (write_macro) cudaMemsetAsync(d->status_dev, 0, 4, d->stream);
+  bool odd = (step & 1) != 0;
+  if (d->desc.strict) pwstrict::launch_step(p, d->desc.storage, d->desc.op, d->desc.les, odd, d->grid, d->stream);
+  else pwfast::launch_step(p, d->desc.storage, d->desc.op, d->desc.les, odd, d->grid, d->stream);
+}
+
+// rampFactor (gpu-solver.ts:119-123) and the f32 rounding of packSolverParams.
+float ramp_speed(const pw_domain *d, uint64_t step) {
+  uint32_t r = d->desc.ramp_steps;
+  if (r == 0) return d->u_in;
+  double factor = step == 0 ? 0.0 : (step >= r ? 1.0 : (double)step / (double)r);
+  return (float)(d->desc.u_in * factor);
+}
+
+int launch_init(pw_domain *d) {
+  float u0 = d->desc.ramp_steps > 0 ? 0.0f : d->u_in;
+  PW_TRY(cudaMemsetAsync(d->f, 0, (size_t)19 * d->stride * d->esize, d->stream));
+  pw::StepParams p = params_for(d, 0, u0, 1);
+  if (d->desc.strict) pwstrict::launch_init(p, d->plane[1], d->partials[1], d->desc.storage, d->grid, d->stream);
+  else pwfast::launch_init(p, d->plane[1], d->partials[1], d->desc.storage, d->grid, d->stream);
+  PW_TRY(cudaGetLastError());
+  return PW_OK;
+}
+
+int ensure_scratch(pw_domain *d) {
+  if (d->scratch) return PW_OK;
+  PW_TRY(cudaMalloc(&d->scratch, (size_t)19 * d->cells * 4));
+  return PW_OK;
+}
+
+bool alive(const pw_domain *d) {
+  if (!d) { set_error("The solver handle is NULL."); return false; }
+  return true;
+}
+
+void drop_graphs(pw_domain *d) {
+  for (auto &kv : d->graphs) cudaGraphExecDestroy(kv.second);
+  d->graphs.clear();
+}
+
+// A captured run of kGraphChunk steps beginning at an odd (parity 1) or even step.
+cudaGraphExec_t graph_for(pw_domain *d, int start_parity, int macro_last) {
+  auto key = std::make_pair(start_parity, macro_last);
+  auto it = d->graphs.find(key);
+  if (it != d->graphs.end()) return it->second;
+  cudaStream_t cap;
+  if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t saved = d->stream;
+  d->stream = cap;
+  if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    for (int k = 0; k < kGraphChunk; k++) {
+      uint64_t step = (uint64_t)start_parity + (uint64_t)k;  // only the parity matters
+      enqueue_step(d, step == 0 ? 2 : step, d->u_in, macro_last && k == kGraphChunk - 1);
+    }
+    if (cudaStreamEndCapture(cap, &graph) == cudaSuccess && graph) {
+      if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) exec = nullptr;
+      cudaGraphDestroy(graph);
+    }
+  }
+  d->stream = saved;
+  cudaStreamDestroy(cap);
+  cudaGetLastError();
+  if (exec) d->graphs[key] = exec;
+  return exec;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain **out) {
+  if (!desc || !grid || !out) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  *out = nullptr;
+  if (desc->nx != grid->nx || desc->ny != grid->ny || desc->nz != grid->nz) {
+    set_error("Geometry must match the solver layout and contain flags and q offsets.");
+    return PW_ERR_INVALID;
+  }
+  if (desc->storage < 0 || desc->storage > 2) { set_error("Unknown population storage."); return PW_ERR_INVALID; }
+  if (desc->op != PW_OP_TRT && desc->op != PW_OP_REG) { set_error("Unknown collision operator."); return PW_ERR_INVALID; }
+  if (desc->walls != PW_WALLS_BB) {
+    set_error("Interpolated (Bouzidi) walls are not available in the in-place kernel; use halfway bounce-back.");
+    return PW_ERR_INVALID;
+  }
+  // packSolverParams (gpu-solver.ts:94-105)
+  float tau0f = (float)desc->tau0;
+  float uin = (float)desc->u_in;
+  float nu = (float)(((double)tau0f - 0.5) / 3.0);
+  float shader_tau = (float)((float)(3.0 * (double)nu) + 0.5);
+  if (!std::isfinite(tau0f) || !std::isfinite(shader_tau) || shader_tau <= 0.5f || !std::isfinite(uin)) {
+    set_error("Relaxation time must exceed 0.5 and inlet speed must be finite.");
+    return PW_ERR_INVALID;
+  }
+  size_t cells = grid->cells;
+  if (cells * 19 > 0xffffffffull) { set_error("Population buffers exceed u32 shader indexing."); return PW_ERR_INVALID; }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); set_error("No CUDA device is available."); return PW_ERR_CUDA; }
+
+  pw_domain *d = new pw_domain();
+  d->desc = *desc;
+  d->nx = desc->nx; d->ny = desc->ny; d->nz = desc->nz;
+  d->cells = cells;
+  d->stride = (uint32_t)((cells + 63) / 64 * 64);
+  d->esize = desc->storage == PW_STORE_F32 ? 4 : 2;
+  d->u_in = uin;
+  d->nu = nu;
+  d->cs_term = (float)(18.0 * 1.4142135623730951 * (0.1 * 0.1));
+  d->lambda = 0.1875f;
+  // binary32 constants of the LES-free operator (collide-trt.wgsl:2-4, common.wgsl:116)
+  d->tau0 = 3.0f * nu + 0.5f;
+  d->om_p = 1.0f / d->tau0;
+  d->om_m = 1.0f / (d->lambda / (d->tau0 - 0.5f) + 0.5f);
+  d->grid = dim3((d->nx + pw::kBlockX - 1) / pw::kBlockX, (d->ny + pw::kBlockY - 1) / pw::kBlockY, d->nz);
+  d->nblocks = (size_t)d->grid.x * d->grid.y * d->grid.z;
+  size_t plane_n = (size_t)d->ny * d->nz;
+
+  Allocs a;
+  cudaError_t e = cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&d->force_event, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = a.alloc(&d->f, (size_t)19 * d->stride * d->esize);
+  if (e == cudaSuccess) e = a.alloc((void **)&d->macros, cells * sizeof(float4));
+  if (e == cudaSuccess) e = a.alloc((void **)&d->plane[0], plane_n * sizeof(float4));
+  if (e == cudaSuccess) e = a.alloc((void **)&d->plane[1], plane_n * sizeof(float4));
+  if (e == cudaSuccess) e = a.alloc((void **)&d->flags, cells * 4);
+  if (e == cudaSuccess) e = a.alloc((void **)&d->special, ((cells + 31) / 32 + 1) * 4);
+  if (e == cudaSuccess) e = a.alloc((void **)&d->partials[0], d->nblocks * 3 * sizeof(double));
+  if (e == cudaSuccess) e = a.alloc((void **)&d->partials[1], d->nblocks * 3 * sizeof(double));
+  if (e == cudaSuccess) e = a.alloc((void **)&d->force_dev, 4 * sizeof(double));
+  if (e == cudaSuccess) e = a.alloc((void **)&d->status_dev, 16);
+  if (e == cudaSuccess) e = a.alloc((void **)&d->totals_dev, 4 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMallocHost((void **)&d->force_host, 4 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMallocHost((void **)&d->status_host, 16);
+  if (e != cudaSuccess) {
+    int rc = cuda_status(e, "pw_domain_create");
+    if (d->force_host) cudaFreeHost(d->force_host);
+    if (d->status_host) cudaFreeHost(d->status_host);
+    if (d->force_event) cudaEventDestroy(d->force_event);
+    if (d->stream) cudaStreamDestroy(d->stream);
+    delete d;
+    return rc;
+  }
+  cudaStream_t s = d->stream;
+  unsigned long long *ff = reinterpret_cast<unsigned long long *>(d->totals_dev);
+  unsigned long long none = ~0ull;
+  cudaMemcpyAsync(d->flags, grid->flags, cells * 4, cudaMemcpyDeviceToDevice, s);
+  cudaMemsetAsync(d->partials[0], 0, d->nblocks * 3 * sizeof(double), s);
+  cudaMemsetAsync(d->partials[1], 0, d->nblocks * 3 * sizeof(double), s);
+  cudaMemsetAsync(d->plane[0], 0, plane_n * sizeof(float4), s);
+  cudaMemsetAsync(d->plane[1], 0, plane_n * sizeof(float4), s);
+  cudaMemsetAsync(d->status_dev, 0, 16, s);
+  special_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(d->flags, cells, d->special);
+  cudaMemcpyAsync(ff, &none, 8, cudaMemcpyHostToDevice, s);
+  first_fluid_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(d->flags, cells, ff);
+  cudaMemcpyAsync(&d->first_fluid, ff, 8, cudaMemcpyDeviceToHost, s);
+  int rc = launch_init(d);
+  if (rc == PW_OK) {
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = cuda_status(e, "pw_domain_create init");
+  }
+  if (rc != PW_OK) {
+    cudaFreeHost(d->force_host);
+    cudaFreeHost(d->status_host);
+    cudaEventDestroy(d->force_event);
+    cudaStreamDestroy(d->stream);
+    delete d;
+    return rc;
+  }
+  a.keep = true;
+  *out = d;
+  return PW_OK;
+}
+
+void pw_domain_destroy(pw_domain *d) {
+  if (!d) return;
+  cudaStreamSynchronize(d->stream);
+  drop_graphs(d);
+  cudaFree(d->f); cudaFree(d->macros); cudaFree(d->plane[0]); cudaFree(d->plane[1]);
+  cudaFree(d->flags); cudaFree(d->special); cudaFree(d->partials[0]); cudaFree(d->partials[1]);
+  cudaFree(d->force_dev); cudaFree(d->status_dev); cudaFree(d->totals_dev); cudaFree(d->scratch);
+  cudaFreeHost(d->force_host); cudaFreeHost(d->status_host);
+  cudaEventDestroy(d->force_event);
+  cudaStreamDestroy(d->stream);
+  cudaGetLastError();
+  delete d;
+}
+
+int pw_reset(pw_domain *d) {
+  if (!alive(d)) return PW_ERR_INVALID;
+  int rc = launch_init(d);
+  if (rc != PW_OK) return rc;
+  d->steps = 0;
+  if (d->force_state == FORCE_ENCODED) d->force_state = FORCE_IDLE;  // GpuForce.reset
+  return PW_OK;
+}
+
+int pw_step(pw_domain *d, uint64_t count, int write_macro_on_last) {
+  if (!alive(d)) return PW_ERR_INVALID;
+  if (count > (1ull << 53) || d->steps + count > (1ull << 53)) {
+    set_error("Step count must be a non-negative safe integer.");
+    return PW_ERR_INVALID;
+  }
+  uint64_t k = 0;
+  // ramped steps, one launch each with its own inlet speed
+  while (k < count && d->desc.ramp_steps > 0 && d->steps < d->desc.ramp_steps) {
+    uint64_t step = d->steps + 1;
+    enqueue_step(d, step, ramp_speed(d, step), write_macro_on_last && k == count - 1);
+    d->steps++;
+    k++;
+  }
+  // full-speed steps: graph chunks when the domain is small enough to be launch bound
+  const bool use_graphs = d->cells <= (size_t)8 << 20;
+  while (use_graphs && count - k >= (uint64_t)kGraphChunk) {
+    int macro_last = write_macro_on_last && (count - k == (uint64_t)kGraphChunk);
+    cudaGraphExec_t g = graph_for(d, (int)((d->steps + 1) & 1), macro_last);
+    if (!g) break;
+    if (cudaGraphLaunch(g, d->stream) != cudaSuccess) { cudaGetLastError(); break; }
+    d->steps += kGraphChunk;
+    k += kGraphChunk;
+  }
+  for (; k < count; k++) {
+    uint64_t step = d->steps + 1;
+    enqueue_step(d, step, d->u_in, write_macro_on_last && k == count - 1);
+    d->steps++;
+  }
+  PW_TRY(cudaGetLastError());
+  return PW_OK;
+}
+
+int pw_step_count(const pw_domain *d, uint64_t *out) {
+  if (!d || !out) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  *out = d->steps;
+  return PW_OK;
+}
+
+int pw_encode_force(pw_domain *d) {
+  if (!alive(d)) return PW_ERR_INVALID;
+  if (d->force_state != FORCE_IDLE) return PW_OK;  // occupied slot skips the sample
+  force_reduce_kernel<<<1, 256, 0, d->stream>>>(d->partials[0], d->partials[1], d->nblocks, d->force_dev);
+  PW_TRY(cudaMemcpyAsync(d->force_host, d->force_dev, 3 * sizeof(double), cudaMemcpyDeviceToHost, d->stream));
+  PW_TRY(cudaEventRecord(d->force_event, d->stream));
+  d->force_state = FORCE_ENCODED;
+  d->force_step = d->steps;
+  return PW_OK;
+}
+
+int pw_read_force(pw_domain *d, pw_force_sample *out) {
+  if (!alive(d) || !out) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  if (d->force_state != FORCE_ENCODED) return PW_ERR_BUSY;
+  d->force_state = FORCE_IDLE;
+  PW_TRY(cudaEventSynchronize(d->force_event));
+  out->step = d->force_step;
+  out->fx = d->force_host[0];
+  out->fy = d->force_host[1];
+  out->fz = d->force_host[2];
+  return PW_OK;
+}
+
+int pw_read_macros(pw_domain *d, float *out) {
+  if (!alive(d) || !out) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  PW_TRY(cudaMemcpyAsync(out, d->macros, d->cells * sizeof(float4), cudaMemcpyDeviceToHost, d->stream));
+  PW_TRY(cudaStreamSynchronize(d->stream));
+  return PW_OK;
+}
+
+int pw_write_macros(pw_domain *d, const float *in) {
+  if (!alive(d) || !in) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  PW_TRY(cudaMemcpyAsync(d->macros, in, d->cells * sizeof(float4), cudaMemcpyHostToDevice, d->stream));
+  PW_TRY(cudaStreamSynchronize(d->stream));
+  return PW_OK;
+}
+
+static int read_pops(pw_domain *d, void *out, int mode) {
+  if (!alive(d) || !out) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  int rc = ensure_scratch(d);
+  if (rc != PW_OK) return rc;
+  pw::StepParams p = params_for(d, d->steps, d->u_in, 0);
+  int odd = (int)(d->steps & 1);
+  if (d->desc.strict) pwstrict::launch_read(p, odd, mode, d->scratch, d->desc.storage, d->grid, d->stream);
+  else pwfast::launch_read(p, odd, mode, d->scratch, d->desc.storage, d->grid, d->stream);
+  size_t bytes = (size_t)19 * d->cells * (mode == 0 ? 4 : d->esize);
+  PW_TRY(cudaMemcpyAsync(out, d->scratch, bytes, cudaMemcpyDeviceToHost, d->stream));
+  PW_TRY(cudaStreamSynchronize(d->stream));
+  return PW_OK;
+}
+
+int pw_read_populations(pw_domain *d, float *out) { return read_pops(d, out, 0); }
+int pw_read_populations_raw(pw_domain *d, void *out) { return read_pops(d, out, 1); }
+
+static int write_pops(pw_domain *d, const void *in, int mode) {
+  if (!alive(d) || !in) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  int rc = ensure_scratch(d);
+  if (rc != PW_OK) return rc;
+  size_t bytes = (size_t)19 * d->cells * (mode == 0 ? 4 : d->esize);
+  PW_TRY(cudaMemcpyAsync(d->scratch, in, bytes, cudaMemcpyHostToDevice, d->stream));
+  pw::StepParams p = params_for(d, d->steps, d->u_in, 0);
+  int odd = (int)(d->steps & 1);
+  if (d->desc.strict) {
+    pwstrict::launch_write(p, odd, mode, d->scratch, d->desc.storage, d->grid, d->stream);
+    pwstrict::launch_refresh(p, odd, d->desc.storage, d->grid, d->stream);
+  } else {
+    pwfast::launch_write(p, odd, mode, d->scratch, d->desc.storage, d->grid, d->stream);
+    pwfast::launch_refresh(p, odd, d->desc.storage, d->grid, d->stream);
+  }
+  PW_TRY(cudaStreamSynchronize(d->stream));
+  return PW_OK;
+}
+
+int pw_write_populations(pw_domain *d, const float *g) { return write_pops(d, g, 0); }
+int pw_write_populations_raw(pw_domain *d, const void *raw) { return write_pops(d, raw, 1); }
+
+int pw_read_totals(pw_domain *d, double out[4]) {
+  if (!alive(d) || !out) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  PW_TRY(cudaMemsetAsync(d->totals_dev, 0, 4 * sizeof(double), d->stream));
+  pw::StepParams p = params_for(d, d->steps, d->u_in, 0);
+  int odd = (int)(d->steps & 1);
+  if (d->desc.strict) pwstrict::launch_totals(p, odd, d->totals_dev, d->desc.storage, d->grid, d->stream);
+  else pwfast::launch_totals(p, odd, d->totals_dev, d->desc.storage, d->grid, d->stream);
+  PW_TRY(cudaMemcpyAsync(out, d->totals_dev, 4 * sizeof(double), cudaMemcpyDeviceToHost, d->stream));
+  PW_TRY(cudaStreamSynchronize(d->stream));
+  return PW_OK;
+}
+
+int pw_guard_check(pw_domain *d, int *unstable) {
+  if (!alive(d) || !unstable) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  PW_TRY(cudaMemcpyAsync(d->status_host, d->status_dev, 4, cudaMemcpyDeviceToHost, d->stream));
+  PW_TRY(cudaStreamSynchronize(d->stream));
+  *unstable = (d->status_host[0] & 1u) ? 1 : 0;
+  return PW_OK;
+}
+
+int pw_inject_nan(pw_domain *d) {
+  if (!alive(d)) return PW_ERR_INVALID;
+  if (d->first_fluid == ~0ull) return PW_OK;
+  // The rest population of a cell sits in slot 0 of the cell in both layouts.
+  uint32_t f32nan = 0x7fc00000u;
+  uint16_t h16nan = d->desc.storage == PW_STORE_F16 ? 0x7e00u : 0x7fc0u;
+  char *base = reinterpret_cast<char *>(d->f) + d->first_fluid * d->esize;
+  const void *src = d->esize == 4 ? (const void *)&f32nan : (const void *)&h16nan;
+  PW_TRY(cudaMemcpyAsync(base, src, d->esize, cudaMemcpyHostToDevice, d->stream));
+  PW_TRY(cudaStreamSynchronize(d->stream));
+  return PW_OK;
+}
+
+int pw_domain_buffers(pw_domain *d, void **macros, void **flags, void **stream) {
+  if (!alive(d)) return PW_ERR_INVALID;
+  if (macros) *macros = d->macros;
+  if (flags) *flags = d->flags;
+  if (stream) *stream = d->stream;
+  return PW_OK;
+}
+
+int pw_time_steps(pw_domain *d, uint64_t count, float *ms) {
+  if (!alive(d) || !ms) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  cudaEvent_t a, b;
+  PW_TRY(cudaEventCreate(&a));
+  PW_TRY(cudaEventCreate(&b));
+  cudaEventRecord(a, d->stream);
+  int rc = pw_step(d, count, 0);
+  cudaEventRecord(b, d->stream);
+  cudaError_t e = cudaEventSynchronize(b);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc != PW_OK) return rc;
+  if (e != cudaSuccess) return cuda_status(e, "pw_time_steps");
+  return PW_OK;
+}
+
+}  // extern "C"

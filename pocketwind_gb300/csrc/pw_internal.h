@@ -1,0 +1,56 @@
+// Internal host-side definitions shared by the C-ABI translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/pocketwind.h"
+#include "pw_common.cuh"
+
+namespace pwhost {
+
+void set_error(const char *fmt, ...);
+int cuda_status(cudaError_t e, const char *what);  // PW_ERR_OOM / PW_ERR_CUDA with message
+
+#define PW_TRY(call)                                           \
+  do {                                                         \
+    cudaError_t e_ = (call);                                   \
+    if (e_ != cudaSuccess) return pwhost::cuda_status(e_, #call); \
+  } while (0)
+
+void domain_dims(const pw_domain *d, uint32_t *nx, uint32_t *ny, uint32_t *nz);
+
+// Device-resident packed geometry (the reference's VoxelGrid).
+struct Grid {
+  uint32_t nx = 0, ny = 0, nz = 0;
+  size_t cells = 0;
+  uint32_t *flags = nullptr;      // cells
+  uint32_t *qoff = nullptr;       // cells
+  float *fractions = nullptr;     // nfrac
+  uint32_t *boundary = nullptr;   // nboundary
+  size_t nfrac = 0, nboundary = 0;
+  pw_grid_stats stats{};
+  ~Grid();
+};
+
+// Allocation helper: frees everything it handed out unless released.
+struct Allocs {
+  void *ptrs[32];
+  int n = 0;
+  bool keep = false;
+  cudaError_t alloc(void **p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+    if (e == cudaSuccess) ptrs[n++] = *p;
+    return e;
+  }
+  ~Allocs() {
+    if (!keep)
+      for (int i = 0; i < n; i++) cudaFree(ptrs[i]);
+  }
+};
+
+}  // namespace pwhost
+
+struct pw_grid : pwhost::Grid {};

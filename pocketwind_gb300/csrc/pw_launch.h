@@ -1,0 +1,25 @@
+// Host-side launchers of the stream-collide kernels, one set per build
+// (pwfast: fused multiply-add and simplified algebra; pwstrict: reference order).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "pw_common.cuh"
+
+#define PW_DECLARE_LAUNCHERS(NS)                                                                   \
+  namespace NS {                                                                                   \
+  void launch_step(const pw::StepParams &p, int storage, int op, int les, bool odd, dim3 grid,     \
+                   cudaStream_t s);                                                                \
+  void launch_init(const pw::StepParams &p, float4 *plane_b, double *partials_b, int storage,      \
+                   dim3 grid, cudaStream_t s);                                                     \
+  void launch_read(const pw::StepParams &p, int odd_layout, int mode, void *out, int storage,      \
+                   dim3 grid, cudaStream_t s);                                                     \
+  void launch_write(const pw::StepParams &p, int odd_layout, int mode, const void *in,            \
+                    int storage, dim3 grid, cudaStream_t s);                                       \
+  void launch_refresh(const pw::StepParams &p, int odd_layout, int storage, dim3 grid,             \
+                      cudaStream_t s);                                                             \
+  void launch_totals(const pw::StepParams &p, int odd_layout, double *out, int storage, dim3 grid, \
+                     cudaStream_t s);                                                              \
+  }
+
+PW_DECLARE_LAUNCHERS(pwfast)
+PW_DECLARE_LAUNCHERS(pwstrict)
