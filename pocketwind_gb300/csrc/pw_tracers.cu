@@ -321,7 +321,7 @@ int pw_particles_read(pw_particles *p, float *out) {
 
 void pw_particles_destroy(pw_particles *p) {
   if (!p) return;
-  cudaStreamSynchronize(p->stream);
+  // cudaFree waits for pending work; the owning domain (and its stream) may be gone.
   cudaFree(p->rec);
   delete p;
 }
@@ -379,7 +379,6 @@ int pw_plate_read(pw_plate_smoke *s, float *out) {
 
 void pw_plate_destroy(pw_plate_smoke *s) {
   if (!s) return;
-  cudaStreamSynchronize(s->stream);
   cudaFree(s->smoke);
   cudaFree(s->ports);
   delete s;
@@ -427,7 +426,6 @@ int pw_streaks_read(pw_streaks *s, float *puffs, uint32_t *release_of) {
 
 void pw_streaks_destroy(pw_streaks *s) {
   if (!s) return;
-  cudaStreamSynchronize(s->stream);
   cudaFree(s->puffs);
   cudaFree(s->release_of);
   delete s;

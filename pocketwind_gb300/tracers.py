@@ -31,6 +31,7 @@ def _vp(a):
 
 class Particles:
     def __init__(self, solver: GpuSolver, records: np.ndarray, seed: int, cross_section, fallback):
+        self._ptr = None
         rec = np.ascontiguousarray(records, np.float32).reshape(-1)
         if rec.size % 8:
             raise _lib.RangeError("Particle records hold 8 floats.")
@@ -44,6 +45,7 @@ class Particles:
         self._ptr = out.value
 
     def update(self, steps: float) -> None:
+        self.solver._live()
         _lib.check(_lib.load().pw_particles_update(self._ptr, float(steps)), "particles update")
 
     def write(self, records: np.ndarray) -> None:
@@ -66,15 +68,18 @@ class Particles:
 class PlateSmoke:
     def __init__(self, solver: GpuSolver, plane: int, rake_threads: int = RAKE_THREADS,
                  slots: int = RING_SLOTS, ports=None):
+        self._ptr = None
         pts = np.zeros(0, np.float32) if ports is None else np.ascontiguousarray(ports, np.float32).reshape(-1)
         self.threads = rake_threads + pts.size // 2
         self.slots = slots
         out = C.c_void_p()
+        self.solver = solver  # the plate samples the solver's buffers: keep it alive
         _lib.check(_lib.load().pw_plate_create(solver._live(), int(plane), rake_threads, slots,
                                                _vp(pts) if pts.size else None, pts.size // 2, C.byref(out)), "plate")
         self._ptr = out.value
 
     def advance(self, release: int, releasing: bool, rake) -> None:
+        self.solver._live()
         r = np.array(rake, np.float32)
         _lib.check(_lib.load().pw_plate_advance(self._ptr, int(release), int(bool(releasing)), _vp(r)), "plate advance")
 
@@ -93,13 +98,16 @@ class PlateSmoke:
 
 class Streaks:
     def __init__(self, solver: GpuSolver, ry: int, rz: int, slots: int, rake):
+        self._ptr = None
         r = np.array(rake, np.float32)
         out = C.c_void_p()
         self.n = ry * rz * slots
+        self.solver = solver  # the streaks sample the solver's buffers: keep it alive
         _lib.check(_lib.load().pw_streaks_create(solver._live(), ry, rz, slots, _vp(r), C.byref(out)), "streaks")
         self._ptr = out.value
 
     def advance(self, h_steps: float, release: int, releasing: bool) -> None:
+        self.solver._live()
         _lib.check(_lib.load().pw_streaks_advance(self._ptr, float(h_steps), int(release), int(bool(releasing))),
                    "streaks advance")
 
