@@ -162,6 +162,17 @@ PW_API int pw_write_macros(pw_domain *dom, const float *in);
  * of f16 x 2^15 / bf16) in the same direction-major order. */
 PW_API int pw_read_populations(pw_domain *dom, float *out);
 PW_API int pw_read_populations_raw(pw_domain *dom, void *out);
+/* No counterpart in the reference.  The same decoded readout as
+ * pw_read_populations, but without allocating device memory: for callers that
+ * cannot call cudaMalloc when they read the state back (a GPU whose memory is
+ * already taken by its domains, or a host that budgets device memory once up
+ * front).  pw_read_populations allocates a 19 x cells x 4-byte buffer on first
+ * use; this call converts one direction and a slab of z-planes at a time through
+ * a fixed 4 MiB array in the library's device image, so nx * ny must be at most
+ * 1,048,576 cells (PW_ERR_INVALID otherwise).  Its first call on a device looks
+ * up that array's address and should come before any stream capture; all calls
+ * share the array, so calls that overlap on the GPU race. */
+PW_API int pw_read_populations_noalloc(pw_domain *dom, float *out);
 /* Replace the latest state (decoded deviations, encoded with the storage's
  * rounding, or raw codes).  Used for initial fields and checkpoint restore. */
 PW_API int pw_write_populations(pw_domain *dom, const float *g);

@@ -69,6 +69,7 @@ SIGNATURES = {
     "pw_write_macros": (_int, [_vp, _vp]),
     "pw_read_populations": (_int, [_vp, _vp]),
     "pw_read_populations_raw": (_int, [_vp, _vp]),
+    "pw_read_populations_noalloc": (_int, [_vp, _vp]),
     "pw_write_populations": (_int, [_vp, _vp]),
     "pw_write_populations_raw": (_int, [_vp, _vp]),
     "pw_read_totals": (_int, [_vp, _vp]),

@@ -29,6 +29,7 @@ UNITS = {
     "pw_geometry.cu": ["-fmad=false"],
     "pw_tracers.cu": ["-fmad=false"],
     "pw_domain.cu": [],
+    "pw_noalloc.cu": [],
 }
 HEADERS = ["pw_common.cuh", "pw_lbm.cuh", "pw_launch.h", "pw_internal.h"]
 

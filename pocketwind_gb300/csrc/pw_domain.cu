@@ -101,6 +101,9 @@ namespace pwhost {
 void domain_dims(const pw_domain *d, uint32_t *nx, uint32_t *ny, uint32_t *nz) {
   *nx = d->nx; *ny = d->ny; *nz = d->nz;
 }
+DomainView domain_view(const pw_domain *d) {
+  return DomainView{d->f, d->flags, d->nx, d->ny, d->nz, d->stride, d->steps, d->desc.storage, d->stream};
+}
 }  // namespace pwhost
 
 namespace {

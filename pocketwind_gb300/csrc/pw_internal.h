@@ -22,6 +22,17 @@ int cuda_status(cudaError_t e, const char *what);  // PW_ERR_OOM / PW_ERR_CUDA w
 
 void domain_dims(const pw_domain *d, uint32_t *nx, uint32_t *ny, uint32_t *nz);
 
+// Read-only view of a domain's device state for kernels outside pw_domain.cu.
+struct DomainView {
+  void *f;
+  const uint32_t *flags;
+  uint32_t nx, ny, nz, stride;
+  uint64_t steps;
+  int storage;
+  cudaStream_t stream;
+};
+DomainView domain_view(const pw_domain *d);
+
 // Device-resident packed geometry (the reference's VoxelGrid).
 struct Grid {
   uint32_t nx = 0, ny = 0, nz = 0;
