@@ -68,7 +68,12 @@ typedef struct {
   uint32_t ramp_steps;  /* inlet ramp length; 0 starts at full speed (rampFactor, :119-123) */
   int strict;           /* 1: binary32 evaluated in the reference's order without fused
                            multiply-add, so results match a binary32 restatement bit for bit */
+  int kernel;           /* PW_KERNEL_AUTO: shared-memory staged rows when nx * element bytes is a
+                           multiple of 16 (fast build), else one cell per thread;
+                           PW_KERNEL_CELL: always one cell per thread */
 } pw_domain_desc;
+
+enum { PW_KERNEL_AUTO = 0, PW_KERNEL_CELL = 1 };
 
 /* VoxelGrid statistics (src/geometry/voxel-grid.ts:7-15). */
 typedef struct {

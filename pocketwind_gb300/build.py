@@ -31,7 +31,7 @@ UNITS = {
     "pw_domain.cu": [],
     "pw_noalloc.cu": [],
 }
-HEADERS = ["pw_common.cuh", "pw_lbm.cuh", "pw_launch.h", "pw_internal.h"]
+HEADERS = ["pw_common.cuh", "pw_lbm.cuh", "pw_lbm_tile.cuh", "pw_launch.h", "pw_internal.h"]
 
 
 def nvcc() -> str:

@@ -16,12 +16,13 @@
 //   Odd step  (reads E): g_i(n) = slot opp(i) of n - c_i; writes P(j,n) to slot j of n + c_j.
 //   Even step (reads O): g_i(n) = slot i of n;            writes P(j,n) to slot opp(j) of n.
 // Each cell reads exactly the slots it writes, so the update is race free.
-// Halfway bounce-back: a wall cell w never runs; its slots are mailboxes.  For a
-// fluid cell n with wall link i (w = n - c_i) the odd step needs P(opp(i), n)
-// at slot opp(i) of w: the even step stores it there as well, and the odd
-// step's ordinary push of P(opp(i), n) lands there by itself.  Only the even
-// step of a boundary cell does extra work (one mailbox read and one write per
-// wall link); the odd step is uniform for every cell.
+// Halfway bounce-back: a wall cell w never runs, so its slots keep what was
+// pushed into them.  For a fluid cell n with wall link i (w = n - c_i) the pull
+// needs P_prev(opp(i), n), which the AA pattern leaves in a slot no cell rewrites
+// during the step that reads it: after an odd step it is the slot opp(i) of w
+// (n's own push), after an even step the slot i of n (n's own write).  So a
+// boundary cell reads those two slots for its wall links and otherwise streams
+// as every other cell; nothing is written twice and walls are never written.
 // The pressure outlet reads its upstream cell's previous state, which the AA
 // update overwrites concurrently, so cells at x = nx-2 publish their velocity
 // (computed exactly as stream_collide.wgsl:83-93 does from the stored codes)
@@ -419,8 +420,10 @@ __global__ void __launch_bounds__(NTHREADS) aa_step(StepParams p) {
           uint32_t src;
           if (ODD) src = (uint32_t)opp_of(i) * S_ + b.at(-cx_of(i), -cy_of(i), -cz_of(i));
           else src = (uint32_t)i * S_ + n;
-          if (!ODD && i > 0 && (flag & (1u << (3 + i))))  // mailbox of wall link i
-            src = (uint32_t)opp_of(i) * S_ + b.at(-cx_of(i), -cy_of(i), -cz_of(i));
+          if (i > 0 && (flag & (1u << (3 + i)))) {  // wall link i: the slot nobody rewrites this step
+            if (ODD) src = (uint32_t)i * S_ + n;
+            else src = (uint32_t)opp_of(i) * S_ + b.at(-cx_of(i), -cy_of(i), -cz_of(i));
+          }
           g[i] = S::decode(f[src]);
         }
 #if PW_STRICT
@@ -450,14 +453,12 @@ __global__ void __launch_bounds__(NTHREADS) aa_step(StepParams p) {
         f[dst] = code[j];
       }
       if (flag >> 3) {
-        // Wall links: even steps also fill the mailbox the next odd step reads;
         // SOLID links add 2 c_j g*_j to the drag (force.wgsl:20-29, halfway walls).
 #pragma unroll
         for (int i = 1; i < 19; i++) {
           if (!(flag & (1u << (3 + i)))) continue;
           const int j = opp_of(i);
           const uint32_t w = b.at(-cx_of(i), -cy_of(i), -cz_of(i));
-          if (!ODD) f[(uint32_t)j * S_ + w] = code[j];
           if ((__ldg(&p.flags[w]) & 7u) == SOLID) {
             float v = S::decode(code[j]);
             double term = (double)(v + v);
@@ -477,63 +478,92 @@ __global__ void __launch_bounds__(NTHREADS) aa_step(StepParams p) {
 
 // ---------------------------------------------------------------- init (layout E)
 // init.wgsl:1-8 into the even layout, after the array was cleared: equilibrium
-// at u_start in fluid and EQ cells, macros everywhere (walls at rest), mailboxes,
+// at u_start in fluid and EQ cells, macros everywhere (walls at rest),
 // both outlet planes and both force partials of the start state.
 template <int ST>
-__global__ void __launch_bounds__(NTHREADS) aa_init(StepParams p, float4 *plane_b, double *partials_b) {
+__device__ __forceinline__ void init_cell(const StepParams &p, uint32_t x, uint32_t y, uint32_t z, float4 *plane_b,
+                                          double &fx, double &fy, double &fz, bool &any) {
   using S = Store<ST>;
   using T = typename S::T;
   T *f = reinterpret_cast<T *>(p.f);
-  const uint32_t x = blockIdx.x * BX + threadIdx.x;
-  const uint32_t y = blockIdx.y * BY + threadIdx.y;
-  const uint32_t z = blockIdx.z;
-  bool force_any = false;
-  double fx = 0, fy = 0, fz = 0;
-  if (x < p.nx && y < p.ny) {
-    const uint32_t n = x + p.nx * (y + p.ny * z);
-    const uint32_t flag = p.flags[n];
-    const uint32_t kind = flag & 7u;
-    const Nbr b = make_nbr(p, x, y, z);
-    const float vx = is_wall_kind(kind) ? 0.0f : p.u_in;
-    T code[19];
+  const uint32_t n = x + p.nx * (y + p.ny * z);
+  const uint32_t flag = p.flags[n];
+  const uint32_t kind = flag & 7u;
+  const Nbr b = make_nbr(p, x, y, z);
+  const float vx = is_wall_kind(kind) ? 0.0f : p.u_in;
+  T code[19];
 #pragma unroll
-    for (int j = 0; j < 19; j++) code[j] = S::encode(geq_ref(j, 0.0f, vx, 0.f, 0.f), (uint32_t)j, n);
-    if (!is_wall_kind(kind)) {
+  for (int j = 0; j < 19; j++) code[j] = S::encode(geq_ref(j, 0.0f, vx, 0.f, 0.f), (uint32_t)j, n);
+  if (!is_wall_kind(kind)) {
 #pragma unroll
-      for (int j = 0; j < 19; j++) f[(uint32_t)opp_of(j) * p.stride + n] = code[j];
-      if (kind == FLUID && (flag >> 3)) {
+    for (int j = 0; j < 19; j++) f[(uint32_t)opp_of(j) * p.stride + n] = code[j];
+    if (kind == FLUID && (flag >> 3)) {
 #pragma unroll
-        for (int i = 1; i < 19; i++) {
-          if (!(flag & (1u << (3 + i)))) continue;
-          const int j = opp_of(i);
-          const uint32_t w = b.at(-cx_of(i), -cy_of(i), -cz_of(i));
-          f[(uint32_t)j * p.stride + w] = code[j];
-          if ((p.flags[w] & 7u) == SOLID) {
-            float v = S::decode(code[j]);
-            double term = (double)(v + v);
-            fx += (double)cx_of(j) * term;
-            fy += (double)cy_of(j) * term;
-            fz += (double)cz_of(j) * term;
-            force_any = true;
-          }
+      for (int i = 1; i < 19; i++) {
+        if (!(flag & (1u << (3 + i)))) continue;
+        const int j = opp_of(i);
+        const uint32_t w = b.at(-cx_of(i), -cy_of(i), -cz_of(i));
+        if ((p.flags[w] & 7u) == SOLID) {
+          float v = S::decode(code[j]);
+          double term = (double)(v + v);
+          fx += (double)cx_of(j) * term;
+          fy += (double)cy_of(j) * term;
+          fz += (double)cz_of(j) * term;
+          any = true;
         }
       }
     }
-    p.macros[n] = make_float4(1.0f + 0.0f, vx, 0.f, 0.f);
-    if (x + 2 == p.nx) {
-      float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (!is_wall_kind(kind)) u = outlet_velocity_of<ST>(code);
-      p.plane_out[y + p.ny * z] = u;
-      plane_b[y + p.ny * z] = u;
+  }
+  p.macros[n] = make_float4(1.0f + 0.0f, vx, 0.f, 0.f);
+  if (x + 2 == p.nx) {
+    float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (!is_wall_kind(kind)) u = outlet_velocity_of<ST>(code);
+    p.plane_out[y + p.ny * z] = u;
+    plane_b[y + p.ny * z] = u;
+  }
+}
+
+__device__ __forceinline__ void copy_partial(double *partials_a, double *partials_b) {
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    size_t blk = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * blockIdx.z);
+    for (int k = 0; k < 3; k++) partials_b[3 * blk + k] = partials_a[3 * blk + k];
+  }
+}
+
+// Tile mapping of aa_step: one cell per thread, 32 x 4 cells per block.
+template <int ST>
+__global__ void __launch_bounds__(NTHREADS) aa_init(StepParams p, float4 *plane_b, double *partials_b) {
+  const uint32_t x = blockIdx.x * BX + threadIdx.x;
+  const uint32_t y = blockIdx.y * BY + threadIdx.y;
+  const uint32_t z = blockIdx.z;
+  bool any = false;
+  double fx = 0, fy = 0, fz = 0;
+  if (x < p.nx && y < p.ny) init_cell<ST>(p, x, y, z, plane_b, fx, fy, fz, any);
+  if (__syncthreads_or(any)) {
+    reduce_force(any, fx, fy, fz, p.partials);
+    copy_partial(p.partials, partials_b);
+  }
+}
+
+// Linear mapping of the tiled step: block b owns cells [b * cpb, (b + 1) * cpb).
+template <int ST>
+__global__ void __launch_bounds__(NTHREADS) aa_init_lin(StepParams p, float4 *plane_b, double *partials_b,
+                                                      uint32_t cpb) {
+  const size_t cells = (size_t)p.nx * p.ny * p.nz;
+  bool any = false;
+  double fx = 0, fy = 0, fz = 0;
+  const size_t base = (size_t)blockIdx.x * cpb;
+  for (uint32_t c = threadIdx.x; c < cpb; c += NTHREADS) {
+    size_t n = base + c;
+    if (n < cells) {
+      uint32_t x = (uint32_t)(n % p.nx), y = (uint32_t)((n / p.nx) % p.ny), z = (uint32_t)(n / ((size_t)p.nx * p.ny));
+      init_cell<ST>(p, x, y, z, plane_b, fx, fy, fz, any);
     }
   }
-  if (__syncthreads_or(force_any)) {
-    reduce_force(force_any, fx, fy, fz, p.partials);
-    __syncthreads();
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-      size_t blk = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * blockIdx.z);
-      for (int k = 0; k < 3; k++) partials_b[3 * blk + k] = p.partials[3 * blk + k];
-    }
+  if (__syncthreads_or(any)) {
+    reduce_force(any, fx, fy, fz, p.partials);
+    copy_partial(p.partials, partials_b);
   }
 }
 
@@ -563,8 +593,8 @@ __global__ void aa_read(StepParams p, int odd_layout, int mode, void *out) {
   }
 }
 
-// Write a canonical state into the AA layout of the given parity (plus the
-// mailboxes of even layouts); mode 0 encodes decoded floats, mode 1 copies codes.
+// Write a canonical state into the AA layout of the given parity; mode 0
+// encodes decoded floats, mode 1 copies codes.
 template <int ST>
 __global__ void aa_write(StepParams p, int odd_layout, int mode, const void *in) {
   using S = Store<ST>;
@@ -585,49 +615,64 @@ __global__ void aa_write(StepParams p, int odd_layout, int mode, const void *in)
     T code = mode == 0 ? S::encode(reinterpret_cast<const float *>(in)[k], (uint32_t)j, n)
                        : reinterpret_cast<const T *>(in)[k];
     f[odd_layout ? slot_of<true>(b, j, p.stride, n) : slot_of<false>(b, j, p.stride, n)] = code;
-    // even layouts duplicate the population that bounces off a wall link i = opp(j)
-    const int i = opp_of(j);
-    if (!odd_layout && i > 0 && (flag & (1u << (3 + i))))
-      f[(uint32_t)j * p.stride + b.at(-cx_of(i), -cy_of(i), -cz_of(i))] = code;
   }
 }
 
 // Recompute the outlet plane and this parity's force partial from the latest
 // state (after a write-in).
 template <int ST>
-__global__ void __launch_bounds__(NTHREADS) aa_refresh(StepParams p, int odd_layout) {
+__device__ __forceinline__ void refresh_cell(const StepParams &p, int odd_layout, uint32_t x, uint32_t y, uint32_t z,
+                                             double &fx, double &fy, double &fz, bool &any) {
   using S = Store<ST>;
   using T = typename S::T;
   const T *f = reinterpret_cast<const T *>(p.f);
+  const uint32_t n = x + p.nx * (y + p.ny * z);
+  const uint32_t flag = p.flags[n];
+  const Nbr b = make_nbr(p, x, y, z);
+  if (is_wall_kind(flag & 7u)) return;
+  T code[19];
+#pragma unroll
+  for (int j = 0; j < 19; j++)
+    code[j] = f[odd_layout ? slot_of<true>(b, j, p.stride, n) : slot_of<false>(b, j, p.stride, n)];
+  if (x + 2 == p.nx) p.plane_out[y + p.ny * z] = outlet_velocity_of<ST>(code);
+  if ((flag & 7u) == FLUID && (flag >> 3)) {
+#pragma unroll
+    for (int i = 1; i < 19; i++) {
+      if (!(flag & (1u << (3 + i)))) continue;
+      const int j = opp_of(i);
+      if ((p.flags[b.at(-cx_of(i), -cy_of(i), -cz_of(i))] & 7u) != SOLID) continue;
+      float v = S::decode(code[j]);
+      double term = (double)(v + v);
+      fx += (double)cx_of(j) * term;
+      fy += (double)cy_of(j) * term;
+      fz += (double)cz_of(j) * term;
+      any = true;
+    }
+  }
+}
+
+template <int ST>
+__global__ void __launch_bounds__(NTHREADS) aa_refresh(StepParams p, int odd_layout) {
   const uint32_t x = blockIdx.x * BX + threadIdx.x;
   const uint32_t y = blockIdx.y * BY + threadIdx.y;
   const uint32_t z = blockIdx.z;
   bool any = false;
   double fx = 0, fy = 0, fz = 0;
-  if (x < p.nx && y < p.ny) {
-    const uint32_t n = x + p.nx * (y + p.ny * z);
-    const uint32_t flag = p.flags[n];
-    const Nbr b = make_nbr(p, x, y, z);
-    if (!is_wall_kind(flag & 7u)) {
-      T code[19];
-#pragma unroll
-      for (int j = 0; j < 19; j++)
-        code[j] = f[odd_layout ? slot_of<true>(b, j, p.stride, n) : slot_of<false>(b, j, p.stride, n)];
-      if (x + 2 == p.nx) p.plane_out[y + p.ny * z] = outlet_velocity_of<ST>(code);
-      if ((flag & 7u) == FLUID && (flag >> 3)) {
-#pragma unroll
-        for (int i = 1; i < 19; i++) {
-          if (!(flag & (1u << (3 + i)))) continue;
-          const int j = opp_of(i);
-          if ((p.flags[b.at(-cx_of(i), -cy_of(i), -cz_of(i))] & 7u) != SOLID) continue;
-          float v = S::decode(code[j]);
-          double term = (double)(v + v);
-          fx += (double)cx_of(j) * term;
-          fy += (double)cy_of(j) * term;
-          fz += (double)cz_of(j) * term;
-          any = true;
-        }
-      }
+  if (x < p.nx && y < p.ny) refresh_cell<ST>(p, odd_layout, x, y, z, fx, fy, fz, any);
+  reduce_force(any, fx, fy, fz, p.partials);
+}
+
+template <int ST>
+__global__ void __launch_bounds__(NTHREADS) aa_refresh_lin(StepParams p, int odd_layout, uint32_t cpb) {
+  const size_t cells = (size_t)p.nx * p.ny * p.nz;
+  bool any = false;
+  double fx = 0, fy = 0, fz = 0;
+  const size_t base = (size_t)blockIdx.x * cpb;
+  for (uint32_t c = threadIdx.x; c < cpb; c += NTHREADS) {
+    size_t n = base + c;
+    if (n < cells) {
+      uint32_t x = (uint32_t)(n % p.nx), y = (uint32_t)((n / p.nx) % p.ny), z = (uint32_t)(n / ((size_t)p.nx * p.ny));
+      refresh_cell<ST>(p, odd_layout, x, y, z, fx, fy, fz, any);
     }
   }
   reduce_force(any, fx, fy, fz, p.partials);
@@ -700,6 +745,14 @@ void launch_step(const StepParams &p, int storage, int op, int les, bool odd, di
   }
 void launch_init(const StepParams &p, float4 *plane_b, double *partials_b, int storage, dim3 g, cudaStream_t s) {
   PW_DISPATCH(storage, (aa_init<ST><<<g, dim3(BX, BY), 0, s>>>(p, plane_b, partials_b)))
+}
+void launch_init_lin(const StepParams &p, float4 *plane_b, double *partials_b, int storage, unsigned blocks,
+                     uint32_t cpb, cudaStream_t s) {
+  PW_DISPATCH(storage, (aa_init_lin<ST><<<blocks, NTHREADS, 0, s>>>(p, plane_b, partials_b, cpb)))
+}
+void launch_refresh_lin(const StepParams &p, int odd_layout, int storage, unsigned blocks, uint32_t cpb,
+                        cudaStream_t s) {
+  PW_DISPATCH(storage, (aa_refresh_lin<ST><<<blocks, NTHREADS, 0, s>>>(p, odd_layout, cpb)))
 }
 void launch_read(const StepParams &p, int odd_layout, int mode, void *out, int storage, dim3 g, cudaStream_t s) {
   PW_DISPATCH(storage, (aa_read<ST><<<g, dim3(BX, BY), 0, s>>>(p, odd_layout, mode, out)))
