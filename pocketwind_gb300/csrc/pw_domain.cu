@@ -93,7 +93,7 @@ struct pw_domain {
   uint64_t force_step = 0;
   float u_in = 0, nu = 0, cs_term = 0, lambda = 0, tau0 = 0, om_p = 0, om_m = 0;
   dim3 grid;
-  bool tiled = false;             // TMA-staged row tiles (fast build)
+  bool tiled = false;             // TMA-staged row tiles
   uint32_t rows_per_tile = 0;
   unsigned tile_blocks = 0;
   size_t tile_smem = 0;
@@ -137,7 +137,10 @@ void enqueue_step(pw_domain *d, uint64_t step, float u_in, int write_macro) {
   pw::StepParams p = params_for(d, step, u_in, write_macro);
   if (write_macro) cudaMemsetAsync(d->status_dev, 0, 4, d->stream);
   bool odd = (step & 1) != 0;
-  if (d->tiled)
+  if (d->tiled && d->desc.strict)
+    pwstrict::launch_step_tile(p, d->desc.storage, d->desc.op, d->desc.les, odd, d->rows_per_tile, d->tile_blocks,
+                               d->tile_smem, d->stream);
+  else if (d->tiled)
     pwfast::launch_step_tile(p, d->desc.storage, d->desc.op, d->desc.les, odd, d->rows_per_tile, d->tile_blocks,
                              d->tile_smem, d->stream);
   else if (d->desc.strict)
@@ -158,7 +161,10 @@ int launch_init(pw_domain *d) {
   float u0 = d->desc.ramp_steps > 0 ? 0.0f : d->u_in;
   PW_TRY(cudaMemsetAsync(d->f, 0, (size_t)19 * d->stride * d->esize, d->stream));
   pw::StepParams p = params_for(d, 0, u0, 1);
-  if (d->tiled)
+  if (d->tiled && d->desc.strict)
+    pwstrict::launch_init_lin(p, d->plane[1], d->partials[1], d->desc.storage, d->tile_blocks,
+                              d->rows_per_tile * d->nx, d->stream);
+  else if (d->tiled)
     pwfast::launch_init_lin(p, d->plane[1], d->partials[1], d->desc.storage, d->tile_blocks,
                             d->rows_per_tile * d->nx, d->stream);
   else if (d->desc.strict)
@@ -261,11 +267,12 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
   d->grid = dim3((d->nx + pw::kBlockX - 1) / pw::kBlockX, (d->ny + pw::kBlockY - 1) / pw::kBlockY, d->nz);
   d->nblocks = (size_t)d->grid.x * d->grid.y * d->grid.z;
   // Staged row tiles: rows must be whole 16-byte multiples for the bulk copies and fit in shared memory.
-  if (!desc->strict && desc->kernel == PW_KERNEL_AUTO && (d->nx * d->esize) % 16 == 0) {
+  if (desc->kernel == PW_KERNEL_AUTO && (d->nx * d->esize) % 16 == 0) {
     uint32_t rows = d->ny * d->nz;
     uint32_t rpt = pwfast::tile_rows_for(d->nx, rows, desc->storage);
     size_t smem = pwfast::tile_smem_bytes(d->nx, rpt, desc->storage);
-    if (smem <= (size_t)200 << 10 && pwfast::prepare_tile_kernels(smem) == cudaSuccess) {
+    cudaError_t pe = desc->strict ? pwstrict::prepare_tile_kernels(smem) : pwfast::prepare_tile_kernels(smem);
+    if (smem <= (size_t)200 << 10 && pe == cudaSuccess) {
       d->tiled = true;
       d->rows_per_tile = rpt;
       d->tile_smem = smem;
@@ -456,7 +463,10 @@ static int write_pops(pw_domain *d, const void *in, int mode) {
   PW_TRY(cudaMemcpyAsync(d->scratch, in, bytes, cudaMemcpyHostToDevice, d->stream));
   pw::StepParams p = params_for(d, d->steps, d->u_in, 0);
   int odd = (int)(d->steps & 1);
-  if (d->desc.strict) {
+  if (d->desc.strict && d->tiled) {
+    pwstrict::launch_write(p, odd, mode, d->scratch, d->desc.storage, d->grid, d->stream);
+    pwstrict::launch_refresh_lin(p, odd, d->desc.storage, d->tile_blocks, d->rows_per_tile * d->nx, d->stream);
+  } else if (d->desc.strict) {
     pwstrict::launch_write(p, odd, mode, d->scratch, d->desc.storage, d->grid, d->stream);
     pwstrict::launch_refresh(p, odd, d->desc.storage, d->grid, d->stream);
   } else if (d->tiled) {

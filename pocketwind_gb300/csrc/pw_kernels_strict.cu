@@ -5,3 +5,4 @@
 #define PW_STRICT 1
 #define PW_DEFINE_LAUNCHERS
 #include "pw_lbm.cuh"
+#include "pw_lbm_tile.cuh"

@@ -23,17 +23,14 @@
                        unsigned blocks, uint32_t cpb, cudaStream_t s);                             \
   void launch_refresh_lin(const pw::StepParams &p, int odd_layout, int storage, unsigned blocks,   \
                           uint32_t cpb, cudaStream_t s);                                           \
+  /* TMA-staged rows: blocks of 128 threads owning rows_per_tile whole x-rows */                  \
+  uint32_t tile_rows_for(uint32_t nx, uint32_t rows, int storage);                                 \
+  size_t tile_smem_bytes(uint32_t nx, uint32_t rows_per_tile, int storage);                        \
+  cudaError_t prepare_tile_kernels(size_t smem_bytes);                                             \
+  void launch_step_tile(const pw::StepParams &p, int storage, int op, int les, bool odd,           \
+                        uint32_t rows_per_tile, unsigned blocks, size_t smem_bytes, cudaStream_t s); \
   }
 
 PW_DECLARE_LAUNCHERS(pwfast)
 PW_DECLARE_LAUNCHERS(pwstrict)
 
-// The TMA-staged step (fast build): blocks of 128 threads, each owning
-// rows_per_tile whole x-rows; needs nx * element bytes to be a multiple of 16.
-namespace pwfast {
-uint32_t tile_rows_for(uint32_t nx, uint32_t rows, int storage);
-size_t tile_smem_bytes(uint32_t nx, uint32_t rows_per_tile, int storage);
-cudaError_t prepare_tile_kernels(size_t smem_bytes);
-void launch_step_tile(const pw::StepParams &p, int storage, int op, int les, bool odd, uint32_t rows_per_tile,
-                      unsigned blocks, size_t smem_bytes, cudaStream_t s);
-}

@@ -1,8 +1,9 @@
-// TMA-staged form of the fused AA stream-collide (fast build).
+// TMA-staged form of the fused AA stream-collide.
 //
-// Same semantics and per-cell arithmetic as aa_step (pw_lbm.cuh), so its stored
-// codes equal the one-cell-per-thread kernel's bit for bit; only the data
-// movement differs.  A block owns R whole x-rows (consecutive in y, then z).  For
+// Included after pw_lbm.cuh by both builds (PW_NS, PW_STRICT).  Same semantics and
+// per-cell arithmetic as aa_step; only the data movement differs, so the strict
+// build's tile kernel reproduces the binary32 restatement bit for bit like the
+// one-cell-per-thread strict kernel does.  A block owns R whole x-rows (consecutive in y, then z).  For
 // each of the 19 slots s it stages the R rows that its cells pull slot s from --
 // the block's own rows on even steps, the rows shifted by (c_s.y, c_s.z) on odd
 // steps -- with one bulk TMA copy per row (cp.async.bulk, completion counted on
@@ -19,10 +20,9 @@
 //
 // Every wait on the mbarrier is bounded: past the limit the block raises bit 1
 // of the status word, skips its update and returns.
-#pragma once
 #include "pw_common.cuh"
 
-namespace pwfast {
+namespace PW_NS {
 using namespace pw;
 
 constexpr int TILE_THREADS = NTHREADS;  // 128: the force-partial reduction's block size
@@ -192,6 +192,9 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) aa_step_tile(StepParams p, ui
           g[i] = S::decode(f[src]);
         }
       }
+#if PW_STRICT
+      update_ref<OP, LES>(p, g, flag, post, rho, vx, vy, vz);
+#else
       if (LES && (flag >> 3) != 0u) {
         float m4[4];
         wall_cell_update<OP>(p, g, flag, post, m4);
@@ -201,6 +204,7 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) aa_step_tile(StepParams p, ui
 #pragma unroll
         for (int j = 0; j < 19; j++) post[j] = g[j];
       }
+#endif
       if (p.write_macro) {
         bool bad = !(rho >= 0.5f && rho <= 1.5f);
         if (bad) atomicOr(p.status, 1u);
@@ -259,4 +263,67 @@ inline uint32_t tile_rows(uint32_t nx, uint32_t rows, size_t elem_bytes, size_t 
   return (uint32_t)r;
 }
 
-}  // namespace pwfast
+#ifdef PW_DEFINE_LAUNCHERS
+static size_t elem_bytes(int storage) { return storage == STORE_F32 ? 4 : 2; }
+
+uint32_t tile_rows_for(uint32_t nx, uint32_t rows, int storage) {
+  return tile_rows(nx, rows, elem_bytes(storage), (size_t)40 << 10);
+}
+
+size_t tile_smem_bytes(uint32_t nx, uint32_t rows_per_tile, int storage) {
+  return 19 * (size_t)rows_per_tile * nx * elem_bytes(storage);
+}
+
+template <int ST, int OP, bool LES>
+static cudaError_t allow_smem(size_t bytes) {
+  cudaError_t e = cudaFuncSetAttribute(aa_step_tile<ST, OP, LES, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(aa_step_tile<ST, OP, LES, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)bytes);
+  return e;
+}
+
+template <int ST>
+static cudaError_t allow_smem_all(size_t bytes) {
+  cudaError_t e = allow_smem<ST, OP_TRT, false>(bytes);
+  if (e == cudaSuccess) e = allow_smem<ST, OP_TRT, true>(bytes);
+  if (e == cudaSuccess) e = allow_smem<ST, OP_REG, false>(bytes);
+  if (e == cudaSuccess) e = allow_smem<ST, OP_REG, true>(bytes);
+  return e;
+}
+
+cudaError_t prepare_tile_kernels(size_t smem_bytes) {
+  cudaError_t e = allow_smem_all<STORE_F32>(smem_bytes);
+  if (e == cudaSuccess) e = allow_smem_all<STORE_F16>(smem_bytes);
+  if (e == cudaSuccess) e = allow_smem_all<STORE_BF16>(smem_bytes);
+  return e;
+}
+
+template <int ST, int OP, bool LES>
+static void tile3(const StepParams &p, bool odd, uint32_t rpt, unsigned blocks, size_t smem, cudaStream_t s) {
+  if (odd) aa_step_tile<ST, OP, LES, true><<<blocks, TILE_THREADS, smem, s>>>(p, rpt);
+  else aa_step_tile<ST, OP, LES, false><<<blocks, TILE_THREADS, smem, s>>>(p, rpt);
+}
+template <int ST>
+static void tile2(const StepParams &p, int op, int les, bool odd, uint32_t rpt, unsigned blocks, size_t smem,
+                  cudaStream_t s) {
+  if (op == OP_REG) {
+    if (les) tile3<ST, OP_REG, true>(p, odd, rpt, blocks, smem, s);
+    else tile3<ST, OP_REG, false>(p, odd, rpt, blocks, smem, s);
+  } else {
+    if (les) tile3<ST, OP_TRT, true>(p, odd, rpt, blocks, smem, s);
+    else tile3<ST, OP_TRT, false>(p, odd, rpt, blocks, smem, s);
+  }
+}
+void launch_step_tile(const StepParams &p, int storage, int op, int les, bool odd, uint32_t rpt, unsigned blocks,
+                      size_t smem, cudaStream_t s) {
+  switch (storage) {
+    case STORE_F16: tile2<STORE_F16>(p, op, les, odd, rpt, blocks, smem, s); break;
+    case STORE_BF16: tile2<STORE_BF16>(p, op, les, odd, rpt, blocks, smem, s); break;
+    default: tile2<STORE_F32>(p, op, les, odd, rpt, blocks, smem, s); break;
+  }
+}
+#endif
+
+}  // namespace PW_NS

@@ -285,41 +285,51 @@ def test_invalid_parameters_raise_range_error():
         G.grid_from_arrays(LAYOUT, bad, boundary)
 
 
-def _pair_equal(a, b, precision):
+def _pair_equal(a, b, precision, exact=True):
     view = np.uint32 if precision == "f32" else np.uint16
-    assert np.array_equal(a.populations_raw().view(view), b.populations_raw().view(view))
-    assert np.array_equal(a.macros().view(np.uint32), b.macros().view(np.uint32))
+    if exact:
+        assert np.array_equal(a.populations_raw().view(view), b.populations_raw().view(view))
+        assert np.array_equal(a.macros().view(np.uint32), b.macros().view(np.uint32))
+    else:
+        assert norm_err(a.populations(), b.populations()) < 1e-5
+        assert norm_err(a.macros()[:, 1:], b.macros()[:, 1:]) < 1e-5
     a.encode_force()
     b.encode_force()
     fa, fb = a.read_force(), b.read_force()
-    assert np.allclose([fa.fx, fa.fy, fa.fz], [fb.fx, fb.fy, fb.fz], rtol=1e-13, atol=1e-16)
+    scale = max(F32_EPS, abs(fb.fx), abs(fb.fy), abs(fb.fz))
+    tol = 1e-12 if exact else 1e-4
+    assert max(abs(fa.fx - fb.fx), abs(fa.fy - fb.fy), abs(fa.fz - fb.fz)) / scale < tol
 
 
+@pytest.mark.parametrize("strict", [True, False])
 @pytest.mark.parametrize("precision", ["f32", "f16", "bf16"])
 @pytest.mark.parametrize("op,les", CONFIGS)
-def test_staged_rows_equal_cell_kernel_on_blob(precision, op, les):
+def test_staged_rows_equal_cell_kernel_on_blob(precision, op, les, strict):
     """The TMA-staged kernel moves data differently but runs the same per-cell
-    arithmetic as the one-cell-per-thread kernel: stored codes must agree bit for bit."""
+    arithmetic: in the strict build the stored codes agree bit for bit with the
+    one-cell-per-thread kernel (and so with the binary32 reference)."""
     geometry, boundary = blob_grid("bb")
-    a = make_solver(geometry, boundary, les=les, op=op, precision=precision, kernel="cell")
-    b = make_solver(geometry, boundary, les=les, op=op, precision=precision, kernel="auto")
+    a = make_solver(geometry, boundary, les=les, op=op, precision=precision, strict=strict, kernel="cell")
+    b = make_solver(geometry, boundary, les=les, op=op, precision=precision, strict=strict, kernel="auto")
     for n in (1, 1, 6, 25):
         a.step(n, True)
         b.step(n, True)
-        _pair_equal(a, b, precision)
+        _pair_equal(a, b, precision, exact=strict)
 
 
+@pytest.mark.parametrize("strict", [True, False])
 @pytest.mark.parametrize("precision", ["f32", "f16"])
-def test_staged_rows_equal_cell_kernel_on_vehicle(precision):
+def test_staged_rows_equal_cell_kernel_on_vehicle(precision, strict):
     """Floor, EQ inlet/outlet planes, LES wall cells: 128 x 64 x 64 vehicle case."""
     from pocketwind_gb300 import meshes
     G, S = _pw()
     layout = (128, 64, 64)
     grid = G.voxelize(meshes.vehicle_case_mesh(128, 64), None, layout, True)
     mk = lambda k: S.GpuSolver.create(layout, grid, S.SolverParams(tau0=0.5 + 3 * 0.00625, u_in=0.05, les=True,
-                                                                    operator="reg", precision=precision, kernel=k))
+                                                                    operator="reg", precision=precision,
+                                                                    strict=strict, kernel=k))
     a, b = mk("cell"), mk("auto")
     for n in (1, 3, 60, 200):
         a.step(n, True)
         b.step(n, True)
-        _pair_equal(a, b, precision)
+        _pair_equal(a, b, precision, exact=strict)
