@@ -68,12 +68,13 @@ typedef struct {
   uint32_t ramp_steps;  /* inlet ramp length; 0 starts at full speed (rampFactor, :119-123) */
   int strict;           /* 1: binary32 evaluated in the reference's order without fused
                            multiply-add, so results match a binary32 restatement bit for bit */
-  int kernel;           /* PW_KERNEL_AUTO: shared-memory staged rows when nx * element bytes is a
-                           multiple of 16 (fast build), else one cell per thread;
-                           PW_KERNEL_CELL: always one cell per thread */
+  int kernel;           /* PW_KERNEL_AUTO and PW_KERNEL_CELL: one cell per thread (the faster
+                           kernel on GB300); PW_KERNEL_TILE: whole x-rows staged through
+                           shared memory by bulk copies, which needs nx * element bytes to
+                           be a multiple of 16 (PW_ERR_INVALID otherwise) */
 } pw_domain_desc;
 
-enum { PW_KERNEL_AUTO = 0, PW_KERNEL_CELL = 1 };
+enum { PW_KERNEL_AUTO = 0, PW_KERNEL_CELL = 1, PW_KERNEL_TILE = 2 };
 
 /* VoxelGrid statistics (src/geometry/voxel-grid.ts:7-15). */
 typedef struct {

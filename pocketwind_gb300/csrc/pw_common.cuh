@@ -34,6 +34,13 @@ __host__ __device__ constexpr float w_of(int i) {
 
 __device__ __forceinline__ bool is_wall_kind(uint32_t k) { return k >= SOLID && k <= FLOOR; }
 
+// Positions whose x-neighbours are reached without the periodic wrap in x; a
+// non-special cell there is a plain cell of the fast step (the y and z seams
+// are handled in the plain kernel).
+__host__ __device__ __forceinline__ bool is_plain_position(uint32_t x, uint32_t nx) {
+  return x >= 1u && x + 2u <= nx;
+}
+
 // ------------------------------------------------------------ storage codecs
 // lowbias32 dithering of the discarded bits (src/lbm/shaders/prelude-f16.wgsl:7-22).
 __device__ __forceinline__ uint32_t lowbias32(uint32_t bits, uint32_t i, uint32_t n) {
@@ -44,6 +51,9 @@ __device__ __forceinline__ uint32_t lowbias32(uint32_t bits, uint32_t i, uint32_
   return r;
 }
 
+// Odd per-direction multipliers of the fast build's dither hash.
+__host__ __device__ constexpr uint32_t dither_mul(int i) { return (0x9e3779b1u ^ ((uint32_t)i * 0x85ebca6bu)) | 1u; }
+
 template <int S> struct Store;
 
 template <> struct Store<STORE_F32> {
@@ -51,8 +61,9 @@ template <> struct Store<STORE_F32> {
   static constexpr float kScale = 1.0f;
   static constexpr float kInvScale = 1.0f;
   __device__ __forceinline__ static float decode(float v) { return v; }
+  __device__ __forceinline__ static float raw(float v) { return v; }
   __device__ __forceinline__ static float encode(float v, uint32_t, uint32_t) { return v; }
-  __device__ __forceinline__ static float nan_code() { return __int_as_float(0x7fc00000); }
+  __device__ __forceinline__ static float encode_fast(float v, uint32_t, uint32_t) { return v; }
 };
 
 template <> struct Store<STORE_F16> {
@@ -61,8 +72,27 @@ template <> struct Store<STORE_F16> {
   static constexpr float kInvScale = 1.0f / 32768.0f;
   // Division by a power of two is exact, so this equals f32(h) / 2^15.
   __device__ __forceinline__ static float decode(__half h) { return __half2float(h) * kInvScale; }
+  __device__ __forceinline__ static float raw(__half h) { return __half2float(h); }
+  // The fast build's rounding of a value already multiplied by 2^15: the same
+  // unbiased dithering of the 13 discarded bits (round up with probability
+  // discarded / 2^13, as "add a dither in [0, 2^13) and truncate"), with the
+  // dither taken from a one-multiply hash of (value bits, cell, direction):
+  // the top 13 bits of bits * mj + nk, where mj = dither_mul(i) and
+  // nk = n * 0x9e3779b9.  The truncation is the conversion's round-toward-zero.
+  // Below 2^-14 (stored units) the dither acts on the subnormal step instead,
+  // and values beyond the f16 range saturate at 65504 rather than reaching
+  // infinity (a population of 2, far outside the density guard's bounds).  The
+  // caller passes NaN as the quiet NaN 0x7fc00000, which this keeps.
+  __device__ __forceinline__ static __half encode_fast(float scaled, uint32_t mj, uint32_t nk) {
+    const uint32_t bits = __float_as_uint(scaled);
+    const uint32_t r = bits * mj + nk;
+    return __float2half_rz(__uint_as_float(bits + (r >> 19)));
+  }
   __device__ __forceinline__ static __half encode(float value, uint32_t i, uint32_t n) {
     float scaled = value * kScale;
+    // CUDA's NaN (0x7fffffff) would carry into the sign below and become -0; the
+    // reference's GPUs produce 0x7fc00000, which stays NaN.  Keep NaN a NaN.
+    if (scaled != scaled) return __ushort_as_half((unsigned short)0x7e00u);
     uint32_t bits = __float_as_uint(scaled);
     uint32_t magnitude = bits & 0x7fffffffu;
     if (magnitude < 0x38800000u) return __float2half_rn(scaled);
@@ -78,6 +108,14 @@ template <> struct Store<STORE_BF16> {
   static constexpr float kScale = 1.0f;
   static constexpr float kInvScale = 1.0f;
   __device__ __forceinline__ static float decode(__nv_bfloat16 h) { return __bfloat162float(h); }
+  __device__ __forceinline__ static float raw(__nv_bfloat16 h) { return __bfloat162float(h); }
+  // The fast build's rounding: encode_fast of the f16 codec on the 16 bits that
+  // bfloat16 discards.
+  __device__ __forceinline__ static __nv_bfloat16 encode_fast(float value, uint32_t mj, uint32_t nk) {
+    const uint32_t bits = __float_as_uint(value);
+    const uint32_t r = bits * mj + nk;
+    return __float2bfloat16_rz(__uint_as_float(bits + (r >> 16)));
+  }
   // The f16 dithering rule applied to the 16 bits bfloat16 discards.
   __device__ __forceinline__ static __nv_bfloat16 encode(float value, uint32_t i, uint32_t n) {
     uint32_t bits = __float_as_uint(value);
@@ -110,6 +148,10 @@ struct StepParams {
   float nu, cs_term, lambda;
   float tau0, omega_plus, omega_minus;  // binary32 constants of the LES-free operator
   int write_macro;
+  // Plain cells (no periodic wrap in reach): direction i is loaded from element
+  // n + ld[i] and stored to element n + st[i] of f, offsets for this step's parity.
+  uint32_t ld[19];
+  uint32_t st[19];
 };
 
 }  // namespace pw

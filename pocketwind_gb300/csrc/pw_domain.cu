@@ -37,6 +37,72 @@ __global__ void special_kernel(const uint32_t *flags, size_t cells, uint32_t *sp
   if ((threadIdx.x & 31) == 0 && i < cells) special[i >> 5] = word;
 }
 
+// The fast step's edge list: non-wall cells that are special or on the x faces,
+// except EQ cells without wall links, in ascending cell order (so its force
+// partials sum in a fixed order).
+__device__ __forceinline__ bool is_edge_cell(const uint32_t *flags, const uint32_t *special, uint32_t n, uint32_t nx,
+                                             uint32_t ny, uint32_t nz) {
+  const uint32_t flag = flags[n];
+  if (pw::is_wall_kind(flag & 7u) || flag == pw::EQ) return false;  // EQ without wall links: plain kernels
+  return !pw::is_plain_position(n % nx, nx) || ((special[n >> 5] >> (n & 31u)) & 1u);
+}
+
+constexpr int kEdgeBlock = 1024;
+
+__global__ void edge_count_kernel(const uint32_t *flags, const uint32_t *special, uint32_t nx, uint32_t ny,
+                                  uint32_t nz, uint32_t cells, uint32_t *block_counts) {
+  __shared__ uint32_t warp_counts[kEdgeBlock / 32];
+  const uint32_t n = blockIdx.x * kEdgeBlock + threadIdx.x;
+  const bool pred = n < cells && is_edge_cell(flags, special, n, nx, ny, nz);
+  const uint32_t ballot = __ballot_sync(0xffffffffu, pred);
+  if ((threadIdx.x & 31) == 0) warp_counts[threadIdx.x >> 5] = __popc(ballot);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int w = 0; w < kEdgeBlock / 32; w++) t += warp_counts[w];
+    block_counts[blockIdx.x] = t;
+  }
+}
+
+// Exclusive scan of the block counts in place (one block); total into *total.
+__global__ void edge_scan_kernel(uint32_t *counts, uint32_t nblk, uint32_t *total) {
+  __shared__ uint32_t sh[kEdgeBlock];
+  uint32_t carry = 0;
+  for (uint32_t base = 0; base < nblk; base += kEdgeBlock) {
+    const uint32_t i = base + threadIdx.x;
+    const uint32_t v = i < nblk ? counts[i] : 0u;
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < kEdgeBlock; o <<= 1) {
+      uint32_t add = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0u;
+      __syncthreads();
+      sh[threadIdx.x] += add;
+      __syncthreads();
+    }
+    if (i < nblk) counts[i] = carry + sh[threadIdx.x] - v;
+    carry += sh[kEdgeBlock - 1];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void edge_write_kernel(const uint32_t *flags, const uint32_t *special, uint32_t nx, uint32_t ny,
+                                  uint32_t nz, uint32_t cells, const uint32_t *offsets, uint32_t *list) {
+  __shared__ uint32_t warp_base[kEdgeBlock / 32];
+  const uint32_t n = blockIdx.x * kEdgeBlock + threadIdx.x;
+  const bool pred = n < cells && is_edge_cell(flags, special, n, nx, ny, nz);
+  const uint32_t ballot = __ballot_sync(0xffffffffu, pred);
+  const uint32_t lane = threadIdx.x & 31;
+  if (lane == 0) warp_base[threadIdx.x >> 5] = __popc(ballot);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = offsets[blockIdx.x];
+    for (int w = 0; w < kEdgeBlock / 32; w++) { uint32_t c = warp_base[w]; warp_base[w] = t; t += c; }
+  }
+  __syncthreads();
+  if (pred) list[warp_base[threadIdx.x >> 5] + __popc(ballot & ((1u << lane) - 1u))] = n;
+}
+
 __global__ void first_fluid_kernel(const uint32_t *flags, size_t cells, unsigned long long *out) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < cells && (flags[i] & 7u) == pw::FLUID) atomicMin(out, (unsigned long long)i);
@@ -93,6 +159,10 @@ struct pw_domain {
   uint64_t force_step = 0;
   float u_in = 0, nu = 0, cs_term = 0, lambda = 0, tau0 = 0, om_p = 0, om_m = 0;
   dim3 grid;
+  bool split = false;             // fast build, one cell per thread: plain kernel + edge list
+  uint32_t *edges = nullptr;      // edge cells in ascending order
+  uint32_t edge_count = 0;
+  dim3 plain_grid;                // the cell grid, or empty when no plain position exists
   bool tiled = false;             // TMA-staged row tiles
   uint32_t rows_per_tile = 0;
   unsigned tile_blocks = 0;
@@ -129,6 +199,17 @@ pw::StepParams params_for(const pw_domain *d, uint64_t step, float u_in, int wri
   p.nu = d->nu; p.cs_term = d->cs_term; p.lambda = d->lambda;
   p.tau0 = d->tau0; p.omega_plus = d->om_p; p.omega_minus = d->om_m;
   p.write_macro = write_macro;
+  // Per-direction element offsets of the plain cells.  Even steps read slot i
+  // and write slot opp(j) of the cell itself; odd steps read slot opp(i) of
+  // n - c_i and write slot j of n + c_j.  Every offset is non-negative
+  // (stride >= cells) and n + offset < 19 * stride < 2^32.
+  const int64_t S = d->stride;
+  const int64_t nx = d->nx, nxy = (int64_t)d->nx * d->ny;
+  for (int i = 0; i < 19; i++) {
+    const int64_t off = pw::cx_of(i) + nx * pw::cy_of(i) + nxy * pw::cz_of(i);
+    p.ld[i] = (uint32_t)(par ? pw::opp_of(i) * S - off : i * S);
+    p.st[i] = (uint32_t)(par ? i * S + off : pw::opp_of(i) * S);
+  }
   return p;
 }
 
@@ -146,7 +227,8 @@ void enqueue_step(pw_domain *d, uint64_t step, float u_in, int write_macro) {
   else if (d->desc.strict)
     pwstrict::launch_step(p, d->desc.storage, d->desc.op, d->desc.les, odd, d->grid, d->stream);
   else
-    pwfast::launch_step(p, d->desc.storage, d->desc.op, d->desc.les, odd, d->grid, d->stream);
+    pwfast::launch_step_split(p, d->desc.storage, d->desc.op, d->desc.les, odd, d->plain_grid, d->edges,
+                              d->edge_count, d->stream);
 }
 
 // rampFactor (gpu-solver.ts:119-123) and the f32 rounding of packSolverParams.
@@ -169,8 +251,16 @@ int launch_init(pw_domain *d) {
                             d->rows_per_tile * d->nx, d->stream);
   else if (d->desc.strict)
     pwstrict::launch_init(p, d->plane[1], d->partials[1], d->desc.storage, d->grid, d->stream);
-  else
-    pwfast::launch_init(p, d->plane[1], d->partials[1], d->desc.storage, d->grid, d->stream);
+  else {
+    // the edge list's blocks own the partials: initialise the state, then take
+    // both parities' partials of the start state in that mapping
+    pw::StepParams q = p;
+    q.partials = nullptr;
+    pwfast::launch_init(q, d->plane[1], nullptr, d->desc.storage, d->grid, d->stream);
+    pwfast::launch_refresh_edges(p, 0, d->desc.storage, d->edges, d->edge_count, d->stream);
+    PW_TRY(cudaMemcpyAsync(d->partials[1], d->partials[0], d->nblocks * 3 * sizeof(double),
+                           cudaMemcpyDeviceToDevice, d->stream));
+  }
   PW_TRY(cudaGetLastError());
   return PW_OK;
 }
@@ -219,6 +309,32 @@ cudaGraphExec_t graph_for(pw_domain *d, int start_parity, int macro_last) {
   return exec;
 }
 
+// The fast step's edge list and its launch shapes; nblocks becomes the edge
+// kernel's block count (at least 1), within the partial arrays' allocation.
+int build_edge_list(pw_domain *d, Allocs &a) {
+  const uint32_t cells = (uint32_t)d->cells;
+  const uint32_t nblk = (cells + kEdgeBlock - 1) / kEdgeBlock;
+  uint32_t *counts = nullptr, total = 0;
+  cudaError_t e = cudaMalloc((void **)&counts, ((size_t)nblk + 1) * 4);
+  if (e != cudaSuccess) return cuda_status(e, "pw_domain_create edge list");
+  edge_count_kernel<<<nblk, kEdgeBlock, 0, d->stream>>>(d->flags, d->special, d->nx, d->ny, d->nz, cells, counts);
+  edge_scan_kernel<<<1, kEdgeBlock, 0, d->stream>>>(counts, nblk, counts + nblk);
+  e = cudaMemcpyAsync(&total, counts + nblk, 4, cudaMemcpyDeviceToHost, d->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(d->stream);
+  if (e == cudaSuccess) e = a.alloc((void **)&d->edges, (size_t)total * 4);
+  if (e == cudaSuccess) {
+    edge_write_kernel<<<nblk, kEdgeBlock, 0, d->stream>>>(d->flags, d->special, d->nx, d->ny, d->nz, cells, counts,
+                                                          d->edges);
+    e = cudaStreamSynchronize(d->stream);
+  }
+  cudaFree(counts);
+  if (e != cudaSuccess) return cuda_status(e, "pw_domain_create edge list");
+  d->edge_count = total;
+  d->nblocks = total ? (total + pw::kBlockX * pw::kBlockY - 1) / (pw::kBlockX * pw::kBlockY) : 1;
+  d->plain_grid = d->nx >= 3 ? d->grid : dim3(0, 0, 0);
+  return PW_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -231,6 +347,7 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
     return PW_ERR_INVALID;
   }
   if (desc->storage < 0 || desc->storage > 2) { set_error("Unknown population storage."); return PW_ERR_INVALID; }
+  if (desc->kernel < PW_KERNEL_AUTO || desc->kernel > PW_KERNEL_TILE) { set_error("Unknown kernel choice."); return PW_ERR_INVALID; }
   if (desc->op != PW_OP_TRT && desc->op != PW_OP_REG) { set_error("Unknown collision operator."); return PW_ERR_INVALID; }
   if (desc->walls != PW_WALLS_BB) {
     set_error("Interpolated (Bouzidi) walls are not available in the in-place kernel; use halfway bounce-back.");
@@ -267,26 +384,37 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
   d->grid = dim3((d->nx + pw::kBlockX - 1) / pw::kBlockX, (d->ny + pw::kBlockY - 1) / pw::kBlockY, d->nz);
   d->nblocks = (size_t)d->grid.x * d->grid.y * d->grid.z;
   // Staged row tiles: rows must be whole 16-byte multiples for the bulk copies and fit in shared memory.
-  if (desc->kernel == PW_KERNEL_AUTO && (d->nx * d->esize) % 16 == 0) {
+  if (desc->kernel == PW_KERNEL_TILE) {
+    if ((d->nx * d->esize) % 16 != 0) {
+      set_error("PW_KERNEL_TILE needs nx * element bytes to be a multiple of 16.");
+      delete d;
+      return PW_ERR_INVALID;
+    }
     uint32_t rows = d->ny * d->nz;
     uint32_t rpt = pwfast::tile_rows_for(d->nx, rows, desc->storage);
     size_t smem = pwfast::tile_smem_bytes(d->nx, rpt, desc->storage);
     cudaError_t pe = desc->strict ? pwstrict::prepare_tile_kernels(smem) : pwfast::prepare_tile_kernels(smem);
-    if (smem <= (size_t)200 << 10 && pe == cudaSuccess) {
-      d->tiled = true;
-      d->rows_per_tile = rpt;
-      d->tile_smem = smem;
-      d->tile_blocks = (rows + rpt - 1) / rpt;
-      d->nblocks = d->tile_blocks;
-    }
     cudaGetLastError();
+    if (smem > (size_t)200 << 10 || pe != cudaSuccess) {
+      set_error("PW_KERNEL_TILE: one x-row tile does not fit in shared memory.");
+      delete d;
+      return PW_ERR_INVALID;
+    }
+    d->tiled = true;
+    d->rows_per_tile = rpt;
+    d->tile_smem = smem;
+    d->tile_blocks = (rows + rpt - 1) / rpt;
+    d->nblocks = d->tile_blocks;
   }
   size_t plane_n = (size_t)d->ny * d->nz;
 
   Allocs a;
   cudaError_t e = cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&d->force_event, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = a.alloc(&d->f, (size_t)19 * d->stride * d->esize);
+  // The fast step's two-cell kernel reads (and discards) elements up to
+  // nx * ny + nx + 64 past the 19 direction planes.
+  if (e == cudaSuccess)
+    e = a.alloc(&d->f, ((size_t)19 * d->stride + (size_t)d->nx * d->ny + d->nx + 64) * d->esize);
   if (e == cudaSuccess) e = a.alloc((void **)&d->macros, cells * sizeof(float4));
   if (e == cudaSuccess) e = a.alloc((void **)&d->plane[0], plane_n * sizeof(float4));
   if (e == cudaSuccess) e = a.alloc((void **)&d->plane[1], plane_n * sizeof(float4));
@@ -321,7 +449,12 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
   cudaMemcpyAsync(ff, &none, 8, cudaMemcpyHostToDevice, s);
   first_fluid_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(d->flags, cells, ff);
   cudaMemcpyAsync(&d->first_fluid, ff, 8, cudaMemcpyDeviceToHost, s);
-  int rc = launch_init(d);
+  int rc = PW_OK;
+  if (!d->tiled && !desc->strict) {
+    d->split = true;
+    rc = build_edge_list(d, a);
+  }
+  if (rc == PW_OK) rc = launch_init(d);
   if (rc == PW_OK) {
     e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) rc = cuda_status(e, "pw_domain_create init");
@@ -346,6 +479,7 @@ void pw_domain_destroy(pw_domain *d) {
   cudaFree(d->f); cudaFree(d->macros); cudaFree(d->plane[0]); cudaFree(d->plane[1]);
   cudaFree(d->flags); cudaFree(d->special); cudaFree(d->partials[0]); cudaFree(d->partials[1]);
   cudaFree(d->force_dev); cudaFree(d->status_dev); cudaFree(d->totals_dev); cudaFree(d->scratch);
+  cudaFree(d->edges);
   cudaFreeHost(d->force_host); cudaFreeHost(d->status_host);
   cudaEventDestroy(d->force_event);
   cudaStreamDestroy(d->stream);
@@ -474,7 +608,7 @@ static int write_pops(pw_domain *d, const void *in, int mode) {
     pwfast::launch_refresh_lin(p, odd, d->desc.storage, d->tile_blocks, d->rows_per_tile * d->nx, d->stream);
   } else {
     pwfast::launch_write(p, odd, mode, d->scratch, d->desc.storage, d->grid, d->stream);
-    pwfast::launch_refresh(p, odd, d->desc.storage, d->grid, d->stream);
+    pwfast::launch_refresh_edges(p, odd, d->desc.storage, d->edges, d->edge_count, d->stream);
   }
   PW_TRY(cudaStreamSynchronize(d->stream));
   return PW_OK;

@@ -32,5 +32,13 @@
   }
 
 PW_DECLARE_LAUNCHERS(pwfast)
+namespace pwfast {
+// The fast build's split step: plain cells over plain_grid (the cell grid),
+// then the listed edge cells, whose blocks own the force partials.
+void launch_step_split(const pw::StepParams &p, int storage, int op, int les, bool odd, dim3 plain_grid,
+                       const uint32_t *list, uint32_t count, cudaStream_t s);
+void launch_refresh_edges(const pw::StepParams &p, int odd_layout, int storage, const uint32_t *list,
+                          uint32_t count, cudaStream_t s);
+}
 PW_DECLARE_LAUNCHERS(pwstrict)
 

@@ -211,48 +211,57 @@ __device__ __forceinline__ void update_ref(const StepParams &p, const float *g, 
 }
 
 // ---------------------------------------------------------------- fast math
-// Same operator, fewer instructions: moments as signed direction sums,
-// equilibrium split into even/odd parts per opposite pair, non-equilibrium
-// stress from the second moment minus its closed-form equilibrium value
-// (sum_i w_i c_a c_b g_eq,i = delta_ab rd/3 + rho u_a u_b).
+// Same operator, fewer instructions: moments from the sums s_k and differences
+// d_k of the nine opposite pairs, equilibrium split into even/odd parts per pair,
+// non-equilibrium stress from the second moment minus its closed-form
+// equilibrium value (sum_i w_i c_a c_b g_eq,i = delta_ab rd/3 + rho u_a u_b),
+// reciprocals and square roots from the hardware approximations (a few ulp).
+// g holds populations in units of 1/scale (scale = 2^15 for f16 storage, so the
+// stored codes enter without a multiply); outputs are written back in those units.
+//
+// Pairs k = 1..9 are directions (2k-1, 2k) with velocities
+// x, y, z, x+y, x+z, y+z, x-y, x-z, y-z.
+// Returns the cell's omega+ (binary32), which is finite exactly when the
+// LES relaxation time is.
 template <int OP, bool LES>
-__device__ __forceinline__ void update_fast(const StepParams &p, float *g, float &rho, float &vx,
-                                            float &vy, float &vz) {
-  float rd = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) +
-             ((g[8] + g[9]) + (g[10] + g[11])) + ((g[12] + g[13]) + (g[14] + g[15])) +
-             ((g[16] + g[17]) + g[18]);
-  float jx = ((g[1] - g[2]) + (g[7] - g[8])) + ((g[9] - g[10]) + (g[13] - g[14])) + (g[15] - g[16]);
-  float jy = ((g[3] - g[4]) + (g[7] - g[8])) + ((g[11] - g[12]) + (g[14] - g[13])) + (g[17] - g[18]);
-  float jz = ((g[5] - g[6]) + (g[9] - g[10])) + ((g[11] - g[12]) + (g[16] - g[15])) + (g[18] - g[17]);
+__device__ __forceinline__ float update_fast(const StepParams &p, float *g, float &rho, float &vx, float &vy,
+                                             float &vz, const float scale = 1.0f, const float inv_scale = 1.0f) {
+  float s[10], d[10];
+#pragma unroll
+  for (int k = 1; k <= 9; k++) {
+    s[k] = g[2 * k - 1] + g[2 * k];
+    d[k] = g[2 * k - 1] - g[2 * k];
+  }
+  const float rd = ((g[0] + (s[1] + s[2] + s[3])) + ((s[4] + s[5] + s[6]) + (s[7] + s[8] + s[9]))) * inv_scale;
+  const float jx = (d[1] + d[4]) + (d[5] + d[7]) + d[8];
+  const float jy = (d[2] + d[4]) + (d[6] - d[7]) + d[9];
+  const float jz = (d[3] + d[5]) + (d[6] - d[8]) - d[9];
   rho = 1.0f + rd;
-  float inv = __frcp_rn(rho);
-  vx = jx * inv;
-  vy = jy * inv;
-  vz = jz * inv;
-  float uu = vx * vx + vy * vy + vz * vz;
-  float K = rd - 1.5f * rho * uu;  // rd + rho(-1.5 uu): the cu-free part of the equilibrium
-  float tau_plus = p.tau0, om_p = p.omega_plus, om_m = p.omega_minus;
+  const float inv = __fdividef(1.0f, rho);
+  const float vs = inv * inv_scale;
+  vx = jx * vs;
+  vy = jy * vs;
+  vz = jz * vs;
+  const float uu = vx * vx + vy * vy + vz * vz;
+  const float K = rd - 1.5f * rho * uu;  // rd + rho(-1.5 uu): the cu-free part of the equilibrium
+  float om_p = p.omega_plus, om_m = p.omega_minus;
   float pxx = 0.f, pyy = 0.f, pzz = 0.f, pxy = 0.f, pxz = 0.f, pyz = 0.f;
   if (LES || OP == OP_REG) {
-    float sxx = ((g[1] + g[2]) + (g[7] + g[8])) + ((g[9] + g[10]) + (g[13] + g[14])) + (g[15] + g[16]);
-    float syy = ((g[3] + g[4]) + (g[7] + g[8])) + ((g[11] + g[12]) + (g[13] + g[14])) + (g[17] + g[18]);
-    float szz = ((g[5] + g[6]) + (g[9] + g[10])) + ((g[11] + g[12]) + (g[15] + g[16])) + (g[17] + g[18]);
-    float sxy = (g[7] + g[8]) - (g[13] + g[14]);
-    float sxz = (g[9] + g[10]) - (g[15] + g[16]);
-    float syz = (g[11] + g[12]) - (g[17] + g[18]);
-    float rd3 = rd * (1.0f / 3.0f);
-    pxx = sxx - (rd3 + rho * vx * vx);
-    pyy = syy - (rd3 + rho * vy * vy);
-    pzz = szz - (rd3 + rho * vz * vz);
-    pxy = sxy - rho * vx * vy;
-    pxz = sxz - rho * vx * vz;
-    pyz = syz - rho * vy * vz;
+    const float rd3 = rd * (1.0f / 3.0f);
+    pxx = (s[1] + s[4] + s[5] + s[7] + s[8]) * inv_scale - (rd3 + rho * vx * vx);
+    pyy = (s[2] + s[4] + s[6] + s[7] + s[9]) * inv_scale - (rd3 + rho * vy * vy);
+    pzz = (s[3] + s[5] + s[6] + s[8] + s[9]) * inv_scale - (rd3 + rho * vz * vz);
+    pxy = (s[4] - s[7]) * inv_scale - rho * vx * vy;
+    pxz = (s[5] - s[8]) * inv_scale - rho * vx * vz;
+    pyz = (s[6] - s[9]) * inv_scale - rho * vy * vz;
     if (LES) {
-      float q = pxx * pxx + pyy * pyy + pzz * pzz + 2.0f * (pxy * pxy + pxz * pxz + pyz * pyz);
-      float t0 = p.tau0;
-      tau_plus = 0.5f * (t0 + sqrtf(t0 * t0 + p.cs_term * sqrtf(q) * inv));
-      om_p = __frcp_rn(tau_plus);
-      om_m = __frcp_rn(p.lambda * __frcp_rn(tau_plus - 0.5f) + 0.5f);
+      const float q = pxx * pxx + pyy * pyy + pzz * pzz + 2.0f * (pxy * pxy + pxz * pxz + pyz * pyz);
+      const float t0 = p.tau0;
+      const float norm = q > 0.0f ? q * rsqrtf(q) : 0.0f;
+      const float arg = t0 * t0 + p.cs_term * norm * inv;
+      const float tau_plus = 0.5f * (t0 + arg * rsqrtf(arg));
+      om_p = __fdividef(1.0f, tau_plus);
+      om_m = __fdividef(1.0f, p.lambda * __fdividef(1.0f, tau_plus - 0.5f) + 0.5f);
     }
   }
   if (OP == OP_REG) {
@@ -260,14 +269,14 @@ __device__ __forceinline__ void update_fast(const StepParams &p, float *g, float
     const float tr3 = (pxx + pyy + pzz) * (1.0f / 3.0f);
     const float r3 = 3.0f * rho, r45 = 4.5f * rho;
     // rest
-    g[0] = w_of(0) * (K + c * (-tr3));
+    g[0] = (w_of(0) * scale) * (K + c * (-tr3));
 #define PW_REG_PAIR(I, CU, PROJ)                                        \
   {                                                                     \
     const float cu_ = (CU);                                             \
     const float ev_ = K + r45 * cu_ * cu_ + c * (PROJ);                 \
     const float od_ = r3 * cu_;                                         \
-    g[I] = w_of(I) * (ev_ + od_);                                       \
-    g[I + 1] = w_of(I) * (ev_ - od_);                                   \
+    g[I] = (w_of(I) * scale) * (ev_ + od_);                             \
+    g[I + 1] = (w_of(I) * scale) * (ev_ - od_);                         \
   }
     PW_REG_PAIR(1, vx, pxx - tr3)
     PW_REG_PAIR(3, vy, pyy - tr3)
@@ -282,17 +291,16 @@ __device__ __forceinline__ void update_fast(const StepParams &p, float *g, float
   } else {
     const float r3 = 3.0f * rho, r45 = 4.5f * rho;
     const float hp = 0.5f * om_p, hm = 0.5f * om_m;
-    g[0] = g[0] - om_p * (g[0] - w_of(0) * K);
+    g[0] = g[0] - om_p * (g[0] - (w_of(0) * scale) * K);
 #define PW_TRT_PAIR(I, CU)                                              \
   {                                                                     \
     const float cu_ = (CU);                                             \
-    const float ep_ = w_of(I) * (K + r45 * cu_ * cu_);                  \
-    const float em_ = w_of(I) * (r3 * cu_);                             \
-    const float gi_ = g[I], gj_ = g[I + 1];                             \
-    const float a_ = hp * ((gi_ + gj_) - 2.0f * ep_);                   \
-    const float b_ = hm * ((gi_ - gj_) - 2.0f * em_);                   \
-    g[I] = gi_ - a_ - b_;                                               \
-    g[I + 1] = gj_ - a_ + b_;                                           \
+    const float ep_ = (w_of(I) * scale) * (K + r45 * cu_ * cu_);        \
+    const float em_ = (w_of(I) * scale) * (r3 * cu_);                   \
+    const float a_ = hp * (s[(I + 1) / 2] - 2.0f * ep_);                \
+    const float b_ = hm * (d[(I + 1) / 2] - 2.0f * em_);                \
+    g[I] = g[I] - a_ - b_;                                              \
+    g[I + 1] = g[I + 1] - a_ + b_;                                      \
   }
     PW_TRT_PAIR(1, vx)
     PW_TRT_PAIR(3, vy)
@@ -305,7 +313,132 @@ __device__ __forceinline__ void update_fast(const StepParams &p, float *g, float
     PW_TRT_PAIR(17, vy - vz)
 #undef PW_TRT_PAIR
   }
+  return om_p;
 }
+
+// ---------------------------------------------------------------- two cells at once
+#if !PW_STRICT
+// update_fast on two cells held as the .x and .y lanes of float2 values, with
+// Blackwell's packed binary32 arithmetic (one FADD2 / FMUL2 / FFMA2 per two
+// cells); the reciprocals and square roots stay per lane.  Same formulas and
+// expression order as update_fast.
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, neg2(b)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(__fdividef(1.0f, a.x), __fdividef(1.0f, a.y)); }
+
+// Lanes flagged in eq (bit 0: .x, bit 1: .y) come out at the equilibrium of
+// rho 1 and velocity (eux, euy, euz) instead: their moments are replaced and
+// their relaxation rates set to 1 before the reconstruction.
+template <int OP, bool LES>
+__device__ __forceinline__ float2 update_fast2(const StepParams &p, float2 *g, float2 &rho, float2 &vx, float2 &vy,
+                                               float2 &vz, const float scale, const float inv_scale, uint32_t eq,
+                                               float2 eux, float2 euy, float2 euz) {
+  float2 s[10], d[10];
+#pragma unroll
+  for (int k = 1; k <= 9; k++) {
+    s[k] = add2(g[2 * k - 1], g[2 * k]);
+    d[k] = sub2(g[2 * k - 1], g[2 * k]);
+  }
+  const float2 is = f2(inv_scale);
+  float2 rd = mul2(add2(add2(g[0], add2(add2(s[1], s[2]), s[3])),
+                        add2(add2(add2(s[4], s[5]), s[6]), add2(add2(s[7], s[8]), s[9]))),
+                   is);
+  if (eq & 1u) rd.x = 0.0f;
+  if (eq & 2u) rd.y = 0.0f;
+  const float2 jx = add2(add2(add2(d[1], d[4]), add2(d[5], d[7])), d[8]);
+  const float2 jy = add2(add2(add2(d[2], d[4]), sub2(d[6], d[7])), d[9]);
+  const float2 jz = sub2(add2(add2(d[3], d[5]), sub2(d[6], d[8])), d[9]);
+  rho = add2(f2(1.0f), rd);
+  const float2 inv = rcp2(rho);
+  const float2 vs = mul2(inv, is);
+  vx = mul2(jx, vs);
+  vy = mul2(jy, vs);
+  vz = mul2(jz, vs);
+  if (eq & 1u) { vx.x = eux.x; vy.x = euy.x; vz.x = euz.x; }
+  if (eq & 2u) { vx.y = eux.y; vy.y = euy.y; vz.y = euz.y; }
+  const float2 uu = fma2(vx, vx, fma2(vy, vy, mul2(vz, vz)));
+  const float2 K = fma2(mul2(f2(-1.5f), rho), uu, rd);
+  float2 om_p = f2(p.omega_plus), om_m = f2(p.omega_minus);
+  float2 pxx = f2(0.f), pyy = f2(0.f), pzz = f2(0.f), pxy = f2(0.f), pxz = f2(0.f), pyz = f2(0.f);
+  if (LES || OP == OP_REG) {
+    const float2 rd3 = mul2(rd, f2(1.0f / 3.0f));
+    const float2 rvx = mul2(rho, vx), rvy = mul2(rho, vy), rvz = mul2(rho, vz);
+    pxx = fma2(add2(add2(add2(s[1], s[4]), add2(s[5], s[7])), s[8]), is, neg2(fma2(rvx, vx, rd3)));
+    pyy = fma2(add2(add2(add2(s[2], s[4]), add2(s[6], s[7])), s[9]), is, neg2(fma2(rvy, vy, rd3)));
+    pzz = fma2(add2(add2(add2(s[3], s[5]), add2(s[6], s[8])), s[9]), is, neg2(fma2(rvz, vz, rd3)));
+    pxy = fma2(sub2(s[4], s[7]), is, neg2(mul2(rvx, vy)));
+    pxz = fma2(sub2(s[5], s[8]), is, neg2(mul2(rvx, vz)));
+    pyz = fma2(sub2(s[6], s[9]), is, neg2(mul2(rvy, vz)));
+    if (LES) {
+      const float2 q = fma2(pxx, pxx, fma2(pyy, pyy, fma2(pzz, pzz, mul2(f2(2.0f),
+                           fma2(pxy, pxy, fma2(pxz, pxz, mul2(pyz, pyz)))))));
+      const float t0 = p.tau0;
+      const float2 norm = make_float2(q.x > 0.0f ? q.x * rsqrtf(q.x) : 0.0f, q.y > 0.0f ? q.y * rsqrtf(q.y) : 0.0f);
+      const float2 arg = fma2(f2(p.cs_term), mul2(norm, inv), f2(t0 * t0));
+      const float2 tau_plus = mul2(f2(0.5f), add2(f2(t0), make_float2(arg.x * rsqrtf(arg.x), arg.y * rsqrtf(arg.y))));
+      om_p = rcp2(tau_plus);
+      om_m = rcp2(fma2(f2(p.lambda), rcp2(sub2(tau_plus, f2(0.5f))), f2(0.5f)));
+    }
+  }
+  if (eq & 1u) { om_p.x = 1.0f; om_m.x = 1.0f; }
+  if (eq & 2u) { om_p.y = 1.0f; om_m.y = 1.0f; }
+  const float2 r3 = mul2(f2(3.0f), rho), r45 = mul2(f2(4.5f), rho);
+  if (OP == OP_REG) {
+    const float2 c = fma2(om_p, f2(-4.5f), f2(4.5f));
+    const float2 tr3 = mul2(add2(add2(pxx, pyy), pzz), f2(1.0f / 3.0f));
+    g[0] = mul2(f2(w_of(0) * scale), fma2(c, neg2(tr3), K));
+#define PW_REG_PAIR2(I, CU, PROJ)                                       \
+  {                                                                     \
+    const float2 cu_ = (CU);                                            \
+    const float2 ev_ = fma2(c, (PROJ), fma2(mul2(r45, cu_), cu_, K));   \
+    const float2 od_ = mul2(r3, cu_);                                   \
+    g[I] = mul2(f2(w_of(I) * scale), add2(ev_, od_));                   \
+    g[I + 1] = mul2(f2(w_of(I) * scale), sub2(ev_, od_));               \
+  }
+    const float2 axx = sub2(pxx, tr3), ayy = sub2(pyy, tr3), azz = sub2(pzz, tr3);
+    const float2 txy = sub2(add2(pxx, pyy), tr3), txz = sub2(add2(pxx, pzz), tr3), tyz = sub2(add2(pyy, pzz), tr3);
+    PW_REG_PAIR2(1, vx, axx)
+    PW_REG_PAIR2(3, vy, ayy)
+    PW_REG_PAIR2(5, vz, azz)
+    PW_REG_PAIR2(7, add2(vx, vy), fma2(f2(2.0f), pxy, txy))
+    PW_REG_PAIR2(9, add2(vx, vz), fma2(f2(2.0f), pxz, txz))
+    PW_REG_PAIR2(11, add2(vy, vz), fma2(f2(2.0f), pyz, tyz))
+    PW_REG_PAIR2(13, sub2(vx, vy), fma2(f2(-2.0f), pxy, txy))
+    PW_REG_PAIR2(15, sub2(vx, vz), fma2(f2(-2.0f), pxz, txz))
+    PW_REG_PAIR2(17, sub2(vy, vz), fma2(f2(-2.0f), pyz, tyz))
+#undef PW_REG_PAIR2
+  } else {
+    // TRT on the pair sums and differences: s' = s - om+ (s - 2 e+),
+    // d' = d - om- (d - 2 e-), post = (s' +- d') / 2 (only g[0] is kept).
+    g[0] = fma2(neg2(om_p), fma2(f2(-w_of(0) * scale), K, g[0]), g[0]);
+#define PW_TRT_PAIR2(I, CU)                                             \
+  {                                                                     \
+    const float2 cu_ = (CU);                                            \
+    const float2 ep_ = mul2(f2(w_of(I) * scale), fma2(mul2(r45, cu_), cu_, K)); \
+    const float2 em_ = mul2(f2(w_of(I) * scale), mul2(r3, cu_));        \
+    const float2 sp_ = fma2(neg2(om_p), fma2(f2(-2.0f), ep_, s[(I + 1) / 2]), s[(I + 1) / 2]); \
+    const float2 dp_ = fma2(neg2(om_m), fma2(f2(-2.0f), em_, d[(I + 1) / 2]), d[(I + 1) / 2]); \
+    g[I] = mul2(f2(0.5f), add2(sp_, dp_));                              \
+    g[I + 1] = mul2(f2(0.5f), sub2(sp_, dp_));                          \
+  }
+    PW_TRT_PAIR2(1, vx)
+    PW_TRT_PAIR2(3, vy)
+    PW_TRT_PAIR2(5, vz)
+    PW_TRT_PAIR2(7, add2(vx, vy))
+    PW_TRT_PAIR2(9, add2(vx, vz))
+    PW_TRT_PAIR2(11, add2(vy, vz))
+    PW_TRT_PAIR2(13, sub2(vx, vy))
+    PW_TRT_PAIR2(15, sub2(vx, vz))
+    PW_TRT_PAIR2(17, sub2(vy, vz))
+#undef PW_TRT_PAIR2
+  }
+  return om_p;
+}
+#endif
 
 // ---------------------------------------------------------------- cell addressing
 struct Nbr {
@@ -358,6 +491,7 @@ __device__ __forceinline__ float4 outlet_velocity_of(const typename Store<ST>::T
 
 // Block reduction of the momentum exchange into this block's partial slot.
 __device__ __forceinline__ void reduce_force(bool any, double fx, double fy, double fz, double *partials) {
+  if (partials == nullptr) return;  // uniform: a kernel parameter
   if (!__syncthreads_or(any)) return;
   __shared__ double red[NTHREADS / 32][3];
 #pragma unroll
@@ -381,100 +515,365 @@ __device__ __forceinline__ void reduce_force(bool any, double fx, double fy, dou
 }
 
 // ---------------------------------------------------------------- the step
-// ODD: this step reads layout E and writes layout O; otherwise the reverse.
+// One cell of a step.  ODD: this step reads layout E and writes layout O;
+// otherwise the reverse.  flag is the cell's packed flags (0 for plain fluid).
 template <int ST, int OP, bool LES, bool ODD>
-__global__ void __launch_bounds__(NTHREADS) aa_step(StepParams p) {
+__device__ __forceinline__ void general_cell(const StepParams &p, uint32_t x, uint32_t y, uint32_t z, uint32_t n,
+                                             uint32_t flag, double &fx, double &fy, double &fz, bool &force_any) {
   using S = Store<ST>;
   using T = typename S::T;
   T *f = reinterpret_cast<T *>(p.f);
+  const uint32_t S_ = p.stride;
+  const uint32_t kind = flag & 7u;
+  if (is_wall_kind(kind)) return;
+  const Nbr b = make_nbr(p, x, y, z);
+  float post[19];
+  float rho = 1.0f, vx = 0.f, vy = 0.f, vz = 0.f;
+  if (kind == EQ) {
+    // stream_collide.wgsl:102-107: inlet at u_in, outlet (x = nx-1 > 0) at rho 1
+    // with the upstream velocity published by the previous step.
+    vx = p.u_in;
+    if (x == p.nx - 1 && x > 0) {
+      float4 u = p.plane_in[y + p.ny * z];
+      vx = u.x; vy = u.y; vz = u.z;
+    }
+#pragma unroll
+    for (int i = 0; i < 19; i++) post[i] = geq_ref(i, 0.0f, vx, vy, vz);
+    rho = 1.0f + 0.0f;
+  } else {
+    float g[19];
+#pragma unroll
+    for (int i = 0; i < 19; i++) {
+      uint32_t src;
+      if (ODD) src = (uint32_t)opp_of(i) * S_ + b.at(-cx_of(i), -cy_of(i), -cz_of(i));
+      else src = (uint32_t)i * S_ + n;
+      if (i > 0 && (flag & (1u << (3 + i)))) {  // wall link i: the slot nobody rewrites this step
+        if (ODD) src = (uint32_t)i * S_ + n;
+        else src = (uint32_t)opp_of(i) * S_ + b.at(-cx_of(i), -cy_of(i), -cz_of(i));
+      }
+      g[i] = S::decode(f[src]);
+    }
+#if PW_STRICT
+    update_ref<OP, LES>(p, g, flag, post, rho, vx, vy, vz);
+#else
+    if (LES && (flag >> 3) != 0u) {
+      update_ref<OP, LES>(p, g, flag, post, rho, vx, vy, vz);
+    } else {
+      update_fast<OP, LES>(p, g, rho, vx, vy, vz);
+#pragma unroll
+      for (int i = 0; i < 19; i++) post[i] = g[i];
+    }
+#endif
+    if (p.write_macro) {
+      bool bad = !(rho >= 0.5f && rho <= 1.5f);  // also catches NaN
+      if (bad) atomicOr(p.status, 1u);
+    }
+  }
+  T code[19];
+#pragma unroll
+  for (int j = 0; j < 19; j++) code[j] = S::encode(post[j], (uint32_t)j, n);
+#pragma unroll
+  for (int j = 0; j < 19; j++) {
+    uint32_t dst;
+    if (ODD) dst = (uint32_t)j * S_ + b.at(cx_of(j), cy_of(j), cz_of(j));
+    else dst = (uint32_t)opp_of(j) * S_ + n;
+    f[dst] = code[j];
+  }
+  if (flag >> 3) {
+    // SOLID links add 2 c_j g*_j to the drag (force.wgsl:20-29, halfway walls).
+#pragma unroll
+    for (int i = 1; i < 19; i++) {
+      if (!(flag & (1u << (3 + i)))) continue;
+      const int j = opp_of(i);
+      const uint32_t w = b.at(-cx_of(i), -cy_of(i), -cz_of(i));
+      if ((__ldg(&p.flags[w]) & 7u) == SOLID) {
+        float v = S::decode(code[j]);
+        double term = (double)(v + v);
+        fx += (double)cx_of(j) * term;
+        fy += (double)cy_of(j) * term;
+        fz += (double)cz_of(j) * term;
+        force_any = true;
+      }
+    }
+  }
+  if (p.write_macro) p.macros[n] = make_float4(rho, vx, vy, vz);
+  if (x + 2 == p.nx) p.plane_out[y + p.ny * z] = outlet_velocity_of<ST>(code);
+}
+
+// Every cell, one per thread, 32 x 4 cells per block (the strict build's step).
+template <int ST, int OP, bool LES, bool ODD>
+__global__ void __launch_bounds__(NTHREADS) aa_step(StepParams p) {
   const uint32_t x = blockIdx.x * BX + threadIdx.x;
   const uint32_t y = blockIdx.y * BY + threadIdx.y;
   const uint32_t z = blockIdx.z;
-  const uint32_t S_ = p.stride;
   bool force_any = false;
   double fx = 0.0, fy = 0.0, fz = 0.0;
   if (x < p.nx && y < p.ny) {
     const uint32_t n = x + p.nx * (y + p.ny * z);
     const bool special = (__ldg(&p.special[n >> 5]) >> (n & 31u)) & 1u;
     const uint32_t flag = special ? __ldg(&p.flags[n]) : 0u;
-    const uint32_t kind = flag & 7u;
-    const Nbr b = make_nbr(p, x, y, z);
-    if (!is_wall_kind(kind)) {
-      float post[19];
-      float rho = 1.0f, vx = 0.f, vy = 0.f, vz = 0.f;
-      if (kind == EQ) {
-        // stream_collide.wgsl:102-107: inlet at u_in, outlet (x = nx-1 > 0) at rho 1
-        // with the upstream velocity published by the previous step.
-        vx = p.u_in;
-        if (x == p.nx - 1 && x > 0) {
-          float4 u = p.plane_in[y + p.ny * z];
-          vx = u.x; vy = u.y; vz = u.z;
-        }
-#pragma unroll
-        for (int i = 0; i < 19; i++) post[i] = geq_ref(i, 0.0f, vx, vy, vz);
-        rho = 1.0f + 0.0f;
-      } else {
-        float g[19];
-#pragma unroll
-        for (int i = 0; i < 19; i++) {
-          uint32_t src;
-          if (ODD) src = (uint32_t)opp_of(i) * S_ + b.at(-cx_of(i), -cy_of(i), -cz_of(i));
-          else src = (uint32_t)i * S_ + n;
-          if (i > 0 && (flag & (1u << (3 + i)))) {  // wall link i: the slot nobody rewrites this step
-            if (ODD) src = (uint32_t)i * S_ + n;
-            else src = (uint32_t)opp_of(i) * S_ + b.at(-cx_of(i), -cy_of(i), -cz_of(i));
-          }
-          g[i] = S::decode(f[src]);
-        }
-#if PW_STRICT
-        update_ref<OP, LES>(p, g, flag, post, rho, vx, vy, vz);
-#else
-        if (LES && (flag >> 3) != 0u) {
-          update_ref<OP, LES>(p, g, flag, post, rho, vx, vy, vz);
-        } else {
-          update_fast<OP, LES>(p, g, rho, vx, vy, vz);
-#pragma unroll
-          for (int i = 0; i < 19; i++) post[i] = g[i];
-        }
-#endif
-        if (p.write_macro) {
-          bool bad = !(rho >= 0.5f && rho <= 1.5f);  // also catches NaN
-          if (bad) atomicOr(p.status, 1u);
-        }
-      }
-      T code[19];
-#pragma unroll
-      for (int j = 0; j < 19; j++) code[j] = S::encode(post[j], (uint32_t)j, n);
-#pragma unroll
-      for (int j = 0; j < 19; j++) {
-        uint32_t dst;
-        if (ODD) dst = (uint32_t)j * S_ + b.at(cx_of(j), cy_of(j), cz_of(j));
-        else dst = (uint32_t)opp_of(j) * S_ + n;
-        f[dst] = code[j];
-      }
-      if (flag >> 3) {
-        // SOLID links add 2 c_j g*_j to the drag (force.wgsl:20-29, halfway walls).
-#pragma unroll
-        for (int i = 1; i < 19; i++) {
-          if (!(flag & (1u << (3 + i)))) continue;
-          const int j = opp_of(i);
-          const uint32_t w = b.at(-cx_of(i), -cy_of(i), -cz_of(i));
-          if ((__ldg(&p.flags[w]) & 7u) == SOLID) {
-            float v = S::decode(code[j]);
-            double term = (double)(v + v);
-            fx += (double)cx_of(j) * term;
-            fy += (double)cy_of(j) * term;
-            fz += (double)cz_of(j) * term;
-            force_any = true;
-          }
-        }
-      }
-      if (p.write_macro) p.macros[n] = make_float4(rho, vx, vy, vz);
-      if (x + 2 == p.nx) p.plane_out[y + p.ny * z] = outlet_velocity_of<ST>(code);
-    }
+    general_cell<ST, OP, LES, ODD>(p, x, y, z, n, flag, fx, fy, fz, force_any);
   }
   reduce_force(force_any, fx, fy, fz, p.partials);
 }
+
+#if !PW_STRICT
+// The step of the fast build runs as two launches over disjoint cells; in the
+// in-place pattern each cell reads and writes only its own slots, so the two
+// commute.  aa_step_fast takes the plain cells (not special, 1 <= x <= nx-2):
+// direction i is read from element n + ld[i] and written to element n + st[i],
+// the arithmetic runs in stored units (populations times 2^15 for f16, so the
+// codes enter and leave without a multiply), and 16-bit codes are rounded by
+// encode_fast: the reference's unbiased dithering of the discarded bits, drawn
+// from a cheaper hash.  EQ cells without wall links ride along in the same
+// warps (their stores then share sectors with the row's plain cells).
+// aa_step_edges takes the listed remaining cells (wall links, periodic x faces)
+// through general_cell and owns the force.
+template <int ST, int OP, bool LES, bool ODD>
+__device__ __forceinline__ void plain_cell(const StepParams &p, uint32_t n, uint32_t x, uint32_t y, uint32_t z,
+                                           const uint32_t *ld, const uint32_t *st) {
+  using S = Store<ST>;
+  using T = typename S::T;
+  T *f = reinterpret_cast<T *>(p.f);
+  float g[19];
+#pragma unroll
+  for (int i = 0; i < 19; i++) g[i] = S::raw(f[n + ld[i]]);
+  float rho, vx, vy, vz;
+  const float om = update_fast<OP, LES>(p, g, rho, vx, vy, vz, S::kScale, S::kInvScale);
+  if (ST != STORE_F32 && !(fabsf(rho + om) < INFINITY)) {
+    // a non-finite state is stored as NaN, as the reference's GPUs store it
+#pragma unroll
+    for (int j = 0; j < 19; j++) g[j] = __uint_as_float(0x7fc00000u);
+  }
+  const uint32_t nk = n * 0x9e3779b9u;
+#pragma unroll
+  for (int j = 0; j < 19; j++) f[n + st[j]] = S::encode_fast(g[j], dither_mul(j), nk);
+  if (p.write_macro) {
+    if (!(rho >= 0.5f && rho <= 1.5f)) atomicOr(p.status, 1u);
+    p.macros[n] = make_float4(rho, vx, vy, vz);
+  }
+  if (x + 2 == p.nx) {
+    // the outlet's upstream plane publishes the velocity of its stored codes
+    // (outlet_velocity_of, accumulated as they are read back)
+    // (addresses from the readout map, so the store addresses need not stay live)
+    const Nbr b = make_nbr(p, x, y, z);
+    float mass = 1.0f, mx = 0.f, my = 0.f, mz = 0.f;
+#pragma unroll
+    for (int j = 0; j < 19; j++) {
+      const float v = S::decode(f[slot_of<ODD>(b, j, p.stride, n)]);
+      mass += v;
+      mx += (float)cx_of(j) * v;
+      my += (float)cy_of(j) * v;
+      mz += (float)cz_of(j) * v;
+    }
+    const float inv = __fdividef(1.0f, mass);
+    p.plane_out[y + p.ny * z] = make_float4(mx * inv, my * inv, mz * inv, 0.f);
+  }
+}
+
+// An EQ cell without wall links (the inlet and outlet planes), in the plain
+// kernels so that its stores share sectors with its row's plain cells:
+// stream_collide.wgsl:102-107 as in general_cell.  Odd steps store to n + c_j,
+// which wraps in x on the faces.
+template <int ST, bool ODD>
+__device__ __forceinline__ void eq_cell(const StepParams &p, uint32_t n, uint32_t x, uint32_t y, uint32_t z,
+                                        const uint32_t *st) {
+  using S = Store<ST>;
+  using T = typename S::T;
+  T *f = reinterpret_cast<T *>(p.f);
+  float vx = p.u_in, vy = 0.f, vz = 0.f;
+  if (x == p.nx - 1 && x > 0) {
+    const float4 u = p.plane_in[y + p.ny * z];
+    vx = u.x; vy = u.y; vz = u.z;
+  }
+  const uint32_t xm = x == 0u ? p.nx : 0u, xp = x + 1u == p.nx ? 0u - p.nx : 0u;
+  const uint32_t nk = n * 0x9e3779b9u;
+#pragma unroll
+  for (int j = 0; j < 19; j++) {
+    const uint32_t o = st[j] + (ODD ? (cx_of(j) < 0 ? xm : (cx_of(j) > 0 ? xp : 0u)) : 0u);
+    f[n + o] = S::encode_fast(geq_ref(j, 0.0f, vx, vy, vz) * S::kScale, dither_mul(j), nk);
+  }
+  if (p.write_macro) p.macros[n] = make_float4(1.0f + 0.0f, vx, vy, vz);
+  if (x + 2 == p.nx) {
+    const Nbr b = make_nbr(p, x, y, z);
+    T code[19];
+#pragma unroll
+    for (int j = 0; j < 19; j++) code[j] = f[slot_of<ODD>(b, j, p.stride, n)];
+    p.plane_out[y + p.ny * z] = outlet_velocity_of<ST>(code);
+  }
+}
+
+// Cells n and n + 32 (x and x + 32 of one row) per thread, the arithmetic in
+// packed pairs and the second cell's elements 32 away from the first's.  ok
+// (bit 0: n, bit 1: n + 32) marks the lanes that are stored: plain cells, and
+// EQ cells without wall links (eq), which take the equilibrium of rho 1 and
+// the inlet or outlet velocity through the same reconstruction
+// (stream_collide.wgsl:102-107).  Other lanes compute on the elements they
+// read (inside the padded array) and store nothing.
+template <int ST, int OP, bool LES, bool ODD>
+__device__ __forceinline__ void plain_pair(const StepParams &p, uint32_t n, uint32_t x, uint32_t y, uint32_t z,
+                                           uint32_t ok, uint32_t eq) {
+  using S = Store<ST>;
+  using T = typename S::T;
+  T *f = reinterpret_cast<T *>(p.f);
+  float2 eux = f2(p.u_in), euy = f2(0.f), euz = f2(0.f);
+  if (eq) {
+    const uint32_t row = y + p.ny * z;
+    if ((eq & 1u) && x == p.nx - 1 && x > 0) {
+      const float4 u = p.plane_in[row];
+      eux.x = u.x; euy.x = u.y; euz.x = u.z;
+    }
+    if ((eq & 2u) && x + 32u == p.nx - 1) {
+      const float4 u = p.plane_in[row];
+      eux.y = u.x; euy.y = u.y; euz.y = u.z;
+    }
+  }
+  float2 g[19];
+#pragma unroll
+  for (int i = 0; i < 19; i++) {
+    const T *a = f + (n + p.ld[i]);
+    g[i] = make_float2(S::raw(a[0]), S::raw(a[32]));
+  }
+  float2 rho, vx, vy, vz;
+  const float2 om = update_fast2<OP, LES>(p, g, rho, vx, vy, vz, S::kScale, S::kInvScale, eq, eux, euy, euz);
+  if (ST != STORE_F32) {
+    // a non-finite state is stored as NaN, as the reference's GPUs store it
+    if (!(fabsf(rho.x + om.x) < INFINITY)) {
+#pragma unroll
+      for (int j = 0; j < 19; j++) g[j].x = __uint_as_float(0x7fc00000u);
+    }
+    if (!(fabsf(rho.y + om.y) < INFINITY)) {
+#pragma unroll
+      for (int j = 0; j < 19; j++) g[j].y = __uint_as_float(0x7fc00000u);
+    }
+  }
+  const uint32_t nk = n * 0x9e3779b9u, nk2 = nk + 32u * 0x9e3779b9u;
+  // EQ lanes at x = 0 or nx - 1 store to n + c_j, which wraps in x on odd steps;
+  // a warp with such a lane takes the wrapping stores as a whole
+  const bool wrap = ODD && __any_sync(__activemask(), eq && (x == 0u || x + 33u >= p.nx));
+  if (!wrap) {
+#pragma unroll
+    for (int j = 0; j < 19; j++) {
+      T *a = f + (n + p.st[j]);
+      if (ok & 1u) a[0] = S::encode_fast(g[j].x, dither_mul(j), nk);
+      if (ok & 2u) a[32] = S::encode_fast(g[j].y, dither_mul(j), nk2);
+    }
+  } else {
+    const uint32_t xa = x, xb = x + 32u;
+#pragma unroll
+    for (int j = 0; j < 19; j++) {
+      const uint32_t wa = cx_of(j) < 0 && xa == 0u ? p.nx : (cx_of(j) > 0 && xa + 1u == p.nx ? 0u - p.nx : 0u);
+      const uint32_t wb = cx_of(j) > 0 && xb + 1u == p.nx ? 0u - p.nx : 0u;
+      if (ok & 1u) f[n + p.st[j] + wa] = S::encode_fast(g[j].x, dither_mul(j), nk);
+      if (ok & 2u) f[n + 32u + p.st[j] + wb] = S::encode_fast(g[j].y, dither_mul(j), nk2);
+    }
+  }
+  if (p.write_macro) {
+    const bool bad_a = (ok & ~eq & 1u) && !(rho.x >= 0.5f && rho.x <= 1.5f);
+    const bool bad_b = (ok & ~eq & 2u) && !(rho.y >= 0.5f && rho.y <= 1.5f);
+    if (bad_a || bad_b) atomicOr(p.status, 1u);
+    if (ok & 1u) p.macros[n] = make_float4(rho.x, vx.x, vy.x, vz.x);
+    if (ok & 2u) p.macros[n + 32] = make_float4(rho.y, vx.y, vy.y, vz.y);
+  }
+  const bool pub_a = (ok & 1u) && x + 2u == p.nx, pub_b = (ok & 2u) && x + 34u == p.nx;
+  if (pub_a || pub_b) {
+    // the outlet's upstream plane publishes the velocity of its stored codes
+    const uint32_t xo = pub_a ? x : x + 32u, no = n + (xo - x);
+    const Nbr b = make_nbr(p, xo, y, z);
+    T code[19];
+#pragma unroll
+    for (int j = 0; j < 19; j++) code[j] = f[slot_of<ODD>(b, j, p.stride, no)];
+    p.plane_out[y + p.ny * z] = outlet_velocity_of<ST>(code);
+  }
+}
+
+// Plain cells and wall-free EQ cells of the whole grid (even steps, which
+// touch only the cell's own slots) or of the rows off the periodic y and z
+// seams (odd steps: y and z from 1 to n-2); threads take x and x + 32 of a
+// 64-cell run of a row.
+template <int ST, int OP, bool LES, bool ODD>
+__global__ void __launch_bounds__(NTHREADS) aa_step_fast(StepParams p) {
+  const uint32_t x = blockIdx.x * (2 * BX) + threadIdx.x;
+  const uint32_t y = blockIdx.y * BY + threadIdx.y + (ODD ? 1u : 0u);
+  const uint32_t z = blockIdx.z + (ODD ? 1u : 0u);
+  if (y + (ODD ? 1u : 0u) >= p.ny) return;
+  const uint32_t n = x + p.nx * (y + p.ny * z);
+  uint32_t ok = 0u, eq = 0u;
+#pragma unroll
+  for (uint32_t k = 0; k < 2u; k++) {
+    const uint32_t xk = x + 32u * k, nk = n + 32u * k;
+    if (xk >= p.nx) continue;
+    if (!((__ldg(&p.special[nk >> 5]) >> (nk & 31u)) & 1u)) {
+      if (is_plain_position(xk, p.nx)) ok |= 1u << k;
+    } else if (__ldg(&p.flags[nk]) == EQ) {
+      ok |= 1u << k;
+      eq |= 1u << k;
+    }
+  }
+  if (ok) plain_pair<ST, OP, LES, ODD>(p, n, x, y, z, ok, eq);
+}
+
+// Odd steps on the seam rows: every row of the planes z = 0 and z = nz-1, then
+// the rows y = 0 and y = ny-1 of the planes between; one row per block row.
+// Neighbour offsets wrap around the domain.
+__host__ __device__ __forceinline__ uint32_t seam_rows(uint32_t ny, uint32_t nz) {
+  const uint32_t zs = nz > 1u ? 2u : 1u, ys = ny > 1u ? 2u : 1u;
+  return zs * ny + (nz - zs) * ys;
+}
+
+template <int ST, int OP, bool LES>
+__global__ void __launch_bounds__(BX) aa_step_seam(StepParams p) {
+  const uint32_t x = blockIdx.x * BX + threadIdx.x;
+  const uint32_t zs = p.nz > 1u ? 2u : 1u, ys = p.ny > 1u ? 2u : 1u;
+  uint32_t r = blockIdx.y, y, z;
+  if (r < zs * p.ny) {
+    z = r < p.ny ? 0u : p.nz - 1u;
+    y = r < p.ny ? r : r - p.ny;
+  } else {
+    r -= zs * p.ny;
+    z = 1u + r / ys;
+    y = (r % ys) ? p.ny - 1u : 0u;
+  }
+  const uint32_t n = x + p.nx * (y + p.ny * z);
+  if (x >= p.nx) return;
+  const bool special = (__ldg(&p.special[n >> 5]) >> (n & 31u)) & 1u;
+  if (special ? __ldg(&p.flags[n]) != EQ : !is_plain_position(x, p.nx)) return;
+  const uint32_t plane = p.nx * p.ny;
+  const uint32_t ym = y == 0u ? p.ny * p.nx : 0u, yp = y + 1u == p.ny ? 0u - p.ny * p.nx : 0u;
+  const uint32_t zm = z == 0u ? p.nz * plane : 0u, zp = z + 1u == p.nz ? 0u - p.nz * plane : 0u;
+  uint32_t ld[19], st[19];
+#pragma unroll
+  for (int i = 0; i < 19; i++) {
+    // loads come from n - c_i, stores go to n + c_i
+    ld[i] = p.ld[i] + (cy_of(i) > 0 ? ym : (cy_of(i) < 0 ? yp : 0u)) + (cz_of(i) > 0 ? zm : (cz_of(i) < 0 ? zp : 0u));
+    st[i] = p.st[i] + (cy_of(i) > 0 ? yp : (cy_of(i) < 0 ? ym : 0u)) + (cz_of(i) > 0 ? zp : (cz_of(i) < 0 ? zm : 0u));
+  }
+  if (special) eq_cell<ST, true>(p, n, x, y, z, st);
+  else plain_cell<ST, OP, LES, true>(p, n, x, y, z, ld, st);
+}
+
+__device__ __forceinline__ void cell_coords(const StepParams &p, uint32_t n, uint32_t &x, uint32_t &y, uint32_t &z) {
+  const uint32_t row = n / p.nx;
+  x = n - row * p.nx;
+  z = row / p.ny;
+  y = row - z * p.ny;
+}
+
+// One listed cell per thread; block b's force partial goes to slot b.
+template <int ST, int OP, bool LES, bool ODD>
+__global__ void __launch_bounds__(NTHREADS) aa_step_edges(StepParams p, const uint32_t *list, uint32_t count) {
+  const uint32_t t = blockIdx.x * NTHREADS + threadIdx.x;
+  bool force_any = false;
+  double fx = 0.0, fy = 0.0, fz = 0.0;
+  if (t < count) {
+    const uint32_t n = __ldg(&list[t]);
+    uint32_t x, y, z;
+    cell_coords(p, n, x, y, z);
+    general_cell<ST, OP, LES, ODD>(p, x, y, z, n, __ldg(&p.flags[n]), fx, fy, fz, force_any);
+  }
+  reduce_force(force_any, fx, fy, fz, p.partials);
+}
+#endif
 
 // ---------------------------------------------------------------- init (layout E)
 // init.wgsl:1-8 into the even layout, after the array was cleared: equilibrium
@@ -524,6 +923,7 @@ __device__ __forceinline__ void init_cell(const StepParams &p, uint32_t x, uint3
 }
 
 __device__ __forceinline__ void copy_partial(double *partials_a, double *partials_b) {
+  if (partials_a == nullptr || partials_b == nullptr) return;
   __syncthreads();
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     size_t blk = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * blockIdx.z);
@@ -678,6 +1078,24 @@ __global__ void __launch_bounds__(NTHREADS) aa_refresh_lin(StepParams p, int odd
   reduce_force(any, fx, fy, fz, p.partials);
 }
 
+#if !PW_STRICT
+// Outlet plane and force partials of the latest state over the fast step's
+// edge list, in aa_step_edges' slot mapping.
+template <int ST>
+__global__ void __launch_bounds__(NTHREADS) aa_refresh_edges(StepParams p, int odd_layout, const uint32_t *list,
+                                                           uint32_t count) {
+  const uint32_t t = blockIdx.x * NTHREADS + threadIdx.x;
+  bool any = false;
+  double fx = 0, fy = 0, fz = 0;
+  if (t < count) {
+    uint32_t x, y, z;
+    cell_coords(p, __ldg(&list[t]), x, y, z);
+    refresh_cell<ST>(p, odd_layout, x, y, z, fx, fy, fz, any);
+  }
+  reduce_force(any, fx, fy, fz, p.partials);
+}
+#endif
+
 // FP64 mass deviation and momentum of the latest state over non-wall cells.
 template <int ST>
 __global__ void __launch_bounds__(NTHREADS) aa_totals(StepParams p, int odd_layout, double *out) {
@@ -722,8 +1140,13 @@ __global__ void __launch_bounds__(NTHREADS) aa_totals(StepParams p, int odd_layo
 template <int ST, int OP, bool LES>
 static void step3(const StepParams &p, bool odd, dim3 g, cudaStream_t s) {
   dim3 blk(BX, BY);
+#if PW_STRICT
   if (odd) aa_step<ST, OP, LES, true><<<g, blk, 0, s>>>(p);
   else aa_step<ST, OP, LES, false><<<g, blk, 0, s>>>(p);
+#else
+  if (odd) aa_step_fast<ST, OP, LES, true><<<g, blk, 0, s>>>(p);
+  else aa_step_fast<ST, OP, LES, false><<<g, blk, 0, s>>>(p);
+#endif
 }
 template <int ST>
 static void step2(const StepParams &p, int op, int les, bool odd, dim3 g, cudaStream_t s) {
@@ -743,6 +1166,45 @@ void launch_step(const StepParams &p, int storage, int op, int les, bool odd, di
     case STORE_BF16: { constexpr int ST = STORE_BF16; CALL; break; } \
     default: { constexpr int ST = STORE_F32; CALL; break; } \
   }
+#if !PW_STRICT
+template <int ST, int OP, bool LES>
+static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *list, uint32_t count, cudaStream_t s) {
+  if (g.x && g.y && g.z) {
+    const unsigned runs = (p.nx + 2 * BX - 1) / (2 * BX);  // 64-cell runs per row
+    if (odd) {
+      dim3 inner(runs, p.ny > 2u ? (p.ny - 2u + BY - 1u) / BY : 0u, p.nz > 2u ? p.nz - 2u : 0u);
+      if (inner.y && inner.z) aa_step_fast<ST, OP, LES, true><<<inner, dim3(BX, BY), 0, s>>>(p);
+      aa_step_seam<ST, OP, LES><<<dim3(g.x, seam_rows(p.ny, p.nz)), BX, 0, s>>>(p);
+    } else {
+      aa_step_fast<ST, OP, LES, false><<<dim3(runs, g.y, g.z), dim3(BX, BY), 0, s>>>(p);
+    }
+  }
+  if (count) {
+    unsigned blocks = (count + NTHREADS - 1) / NTHREADS;
+    if (odd) aa_step_edges<ST, OP, LES, true><<<blocks, NTHREADS, 0, s>>>(p, list, count);
+    else aa_step_edges<ST, OP, LES, false><<<blocks, NTHREADS, 0, s>>>(p, list, count);
+  }
+}
+template <int ST>
+static void step_split2(const StepParams &p, int op, int les, bool odd, dim3 g, const uint32_t *list, uint32_t count,
+                        cudaStream_t s) {
+  if (op == OP_REG) {
+    if (les) step_split3<ST, OP_REG, true>(p, odd, g, list, count, s);
+    else step_split3<ST, OP_REG, false>(p, odd, g, list, count, s);
+  } else {
+    if (les) step_split3<ST, OP_TRT, true>(p, odd, g, list, count, s);
+    else step_split3<ST, OP_TRT, false>(p, odd, g, list, count, s);
+  }
+}
+void launch_step_split(const StepParams &p, int storage, int op, int les, bool odd, dim3 plain_grid,
+                       const uint32_t *list, uint32_t count, cudaStream_t s) {
+  switch (storage) {
+    case STORE_F16: step_split2<STORE_F16>(p, op, les, odd, plain_grid, list, count, s); break;
+    case STORE_BF16: step_split2<STORE_BF16>(p, op, les, odd, plain_grid, list, count, s); break;
+    default: step_split2<STORE_F32>(p, op, les, odd, plain_grid, list, count, s); break;
+  }
+}
+#endif
 void launch_init(const StepParams &p, float4 *plane_b, double *partials_b, int storage, dim3 g, cudaStream_t s) {
   PW_DISPATCH(storage, (aa_init<ST><<<g, dim3(BX, BY), 0, s>>>(p, plane_b, partials_b)))
 }
@@ -750,6 +1212,14 @@ void launch_init_lin(const StepParams &p, float4 *plane_b, double *partials_b, i
                      uint32_t cpb, cudaStream_t s) {
   PW_DISPATCH(storage, (aa_init_lin<ST><<<blocks, NTHREADS, 0, s>>>(p, plane_b, partials_b, cpb)))
 }
+#if !PW_STRICT
+void launch_refresh_edges(const StepParams &p, int odd_layout, int storage, const uint32_t *list, uint32_t count,
+                          cudaStream_t s) {
+  if (!count) return;
+  unsigned blocks = (count + NTHREADS - 1) / NTHREADS;
+  PW_DISPATCH(storage, (aa_refresh_edges<ST><<<blocks, NTHREADS, 0, s>>>(p, odd_layout, list, count)))
+}
+#endif
 void launch_refresh_lin(const StepParams &p, int odd_layout, int storage, unsigned blocks, uint32_t cpb,
                         cudaStream_t s) {
   PW_DISPATCH(storage, (aa_refresh_lin<ST><<<blocks, NTHREADS, 0, s>>>(p, odd_layout, cpb)))

@@ -42,7 +42,7 @@ class SolverParams:
     precision: str = "f32"
     ramp_steps: int = 0
     strict: bool = False
-    kernel: str = "auto"  # "auto" (staged rows where possible) or "cell" (one cell per thread)
+    kernel: str = "auto"  # "auto" or "cell" (one cell per thread), "tile" (x-rows staged in shared memory)
 
 
 @dataclass
@@ -76,7 +76,7 @@ class GpuSolver:
         _lib.require_gpu()
         d = _lib.DomainDesc(nx, ny, nz, float(params.tau0), float(params.u_in), int(bool(params.les)),
                             OPERATORS[params.operator], WALLS[params.walls], PRECISIONS[params.precision],
-                            ramp, int(bool(params.strict)), {"auto": 0, "cell": 1}[params.kernel])
+                            ramp, int(bool(params.strict)), {"auto": 0, "cell": 1, "tile": 2}[params.kernel])
         out = C.c_void_p()
         rc = L.pw_domain_create(C.byref(d), grid._handle.ptr, C.byref(out))
         if rc == _lib.PW_ERR_OOM:
