@@ -15,8 +15,12 @@ e2e     = the same metric through the public solver API the reference's headless
           runner uses (src/app/case-run.ts:154-169): host mesh -> GPU voxelizer ->
           create -> {step 8, encode force, read force} loop, wall clock, with the
           mesh upload (once) and every force readback inside the timed region.
-roofline: algorithmic bytes per cell update B = 2 * 19 * s + 1/8 (s = 2 bytes),
-          achieved = cells * B / mean kernel time, peak = measured HBM copy GB/s.
+roofline: the plain-cell kernels (the two-cell packed-FP32 kernel, and on odd
+          steps its seam-row variant), which update all but the wall-link and
+          x-face cells: algorithmic bytes per cell update B = 2 * 19 * s + 1/8
+          (s = 2 bytes; the 1/8 is the bit-packed special mask), achieved =
+          their cells * B / their summed CUDA-event time per step, peak =
+          measured HBM copy GB/s.  step_roofline repeats it for whole steps.
 cpu_baseline: the binary64 restatement of the reference's CpuSolver (the
           reference's CPU path; the TypeScript original cannot run here), on all
           host cores, over a bounded number of full-domain steps.
@@ -43,6 +47,15 @@ SCALE = 4.0
 U_IN = 0.05
 NU = U_IN * 40 * SCALE / 320  # Re 320 on the body length (40 * SCALE cells)
 TAU0 = 0.5 + 3 * NU
+
+
+def set_size(nx):
+    """The same case at nx x nx/2 x nx/2 with the body scaled by nx/128 (profiling runs)."""
+    global NX, NY, NZ, SCALE, NU, TAU0
+    NX, NY, NZ = nx, nx // 2, nx // 2
+    SCALE = nx / 128
+    NU = U_IN * 40 * SCALE / 320
+    TAU0 = 0.5 + 3 * NU
 METRIC = "D3Q19 MLUPS & % HBM roofline, FP16-store vs FP32, drag err vs FP64 at 1 GB300"
 BYTES = {"f32": 2 * 19 * 4 + 0.125, "f16": 2 * 19 * 2 + 0.125, "bf16": 2 * 19 * 2 + 0.125}
 
@@ -132,7 +145,7 @@ def run_ours(args, rank, world):
     grid = voxelize(body, None, (NX, NY, NZ), True)
     cells = NX * NY * NZ
     results = {}
-    for precision in ("f16", "f32", "bf16"):
+    for precision in args.only.split(","):
         solver = GpuSolver.create((NX, NY, NZ), grid, SolverParams(tau0=TAU0, u_in=U_IN, les=True, operator="reg",
                                                                    precision=precision))
         if isinstance(solver, Exception):
@@ -146,11 +159,15 @@ def run_ours(args, rank, world):
         ms = solver.time_steps(args.steps)
         if precision == "f16":
             clocks = sampler.stop()
+        kernel_ms = solver.profile_steps(min(args.steps, 200)) if precision == "f16" else None
         unstable = False
         solver.step(1, True)
         unstable = solver.guard_unstable()
-        results[precision] = {"ms": ms, "clocks": clocks, "unstable": unstable}
+        results[precision] = {"ms": ms, "clocks": clocks, "unstable": unstable, "kernel_ms": kernel_ms,
+                              "profiled_steps": min(args.steps, 200)}
         solver.destroy()
+    if args.no_e2e:
+        return results, None, 0, body.positions.nbytes, cells, grid
     # end-to-end through the public API (wall clock): mesh upload + voxelize + create + sampled stepping
     import time as _t
     t0 = _t.perf_counter()
@@ -166,6 +183,17 @@ def run_ours(args, rank, world):
     solver.destroy()
     e2e_steps = samples * 8
     return results, e2e_s, e2e_steps, body.positions.nbytes, cells, grid
+
+
+def cell_classes(flags):
+    """Cells updated per step by the plain-cell kernels (plain fluid with
+    1 <= x <= nx-2, and EQ cells without wall links) and by the edge kernel."""
+    import numpy as np
+    kind = flags & 7
+    x = np.arange(flags.size, dtype=np.int64) % NX
+    plain = ((flags == 0) & (x >= 1) & (x <= NX - 2)) | (flags == 4)
+    fluid = (kind == 0) | (kind == 4)
+    return int(plain.sum()), int((fluid & ~plain).sum())
 
 
 def cpu_baseline(grid_flags, steps, threads):
@@ -186,7 +214,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--nx", type=int, default=512, help="profiling runs: the case at nx x nx/2 x nx/2")
+    ap.add_argument("--only", default="f16,f32,bf16", help="profiling runs: storages to time (f16 first)")
+    ap.add_argument("--no-e2e", action="store_true", help="profiling runs: skip the end-to-end leg")
     args = ap.parse_args()
+    if args.nx != 512:
+        set_size(args.nx)
     args.warmup = max(3, args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -207,7 +240,8 @@ def main():
                 "steps": cpu_steps, "warmup": 0, "ms_per_step": round(1000 * dt / cpu_steps, 3),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic", "impl": "reference",
-                "config": {"workload": "vehicle body x4, 512x256x256, REG+LES+wall model, floor", "cells": NX * NY * NZ},
+                "config": {"workload": f"vehicle body x{SCALE:g}, {NX}x{NY}x{NZ}, REG+LES+wall model, floor",
+                           "cells": NX * NY * NZ},
                 "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
                                  "sample": f"{cpu_steps} full-domain steps of the binary64 CpuSolver restatement"},
                 "e2e": {"value": round(mlups, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -231,8 +265,16 @@ def main():
         return
     peak, peak_kind = read_peaks()
     mlups = cells * args.steps * world / (ms * 1e3)
-    achieved = cells * BYTES["f16"] / (ms / args.steps / 1e3) / 1e9
+    step_achieved = cells * BYTES["f16"] / (ms / args.steps / 1e3) / 1e9
+    n_plain, n_edge = cell_classes(grid.flags)
+    kms = results["f16"]["kernel_ms"]
+    prof = results["f16"]["profiled_steps"]
+    plain_s = (kms[0] + kms[1]) / prof / 1e3
+    achieved = n_plain * BYTES["f16"] / plain_s / 1e9
     traffic = read_traffic()
+    first = args.warmup + 1
+    odd_steps = sum(1 for k in range(first, first + args.steps) if k % 2)
+    launches = (args.steps - odd_steps) * (1 + (n_edge > 0)) + odd_steps * (2 + (n_edge > 0))
     line = {
         "metric": METRIC,
         "value": round(mlups, 2),
@@ -246,25 +288,33 @@ def main():
         "vs_baseline": None,
         "dtype": "f32 arithmetic, f16 storage",
         "data": "synthetic (parametric bluff-body mesh)",
-        "config": {"workload": "vehicle body x4, 512x256x256, REG+LES+wall model, floor, FP16 storage",
+        "config": {"workload": f"vehicle body x{SCALE:g}, {NX}x{NY}x{NZ}, REG+LES+wall model, floor, FP16 storage",
                    "cells": cells, "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (2.5 GB populations)"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                     "bytes_per_cell": BYTES["f16"],
-                     "traffic": traffic.get("bytes_per_launch") if traffic else None},
+                     "kernel": "aa_step_fast + aa_step_seam (plain cells, two per thread)",
+                     "bytes_per_cell": BYTES["f16"], "cells_per_step": n_plain,
+                     "ms_per_step": round(plain_s * 1e3, 4),
+                     "traffic": traffic.get("bytes_per_step") if traffic else None,
+                     "traffic_source": traffic.get("source") if traffic else None},
+        "step_roofline": {"achieved": round(step_achieved, 1), "frac": round(step_achieved / peak, 4),
+                          "kernel_shares": {"plain": round(kms[0] / sum(kms), 4), "seam_rows": round(kms[1] / sum(kms), 4),
+                                            "edges": round(kms[2] / sum(kms), 4)},
+                          "edge_cells": n_edge},
         "storage_sweep": {p: {"mlups": round(cells * args.steps / (r["ms"] * 1e3), 2),
                               "hbm_frac": round(cells * BYTES[p] / (r["ms"] / args.steps / 1e3) / 1e9 / peak, 4),
                               "stable": not r["unstable"]}
                           for p, r in results.items()},
-        "e2e": {"value": round(cells * e2e_steps / (e2e_s * 1e6), 2), "unit": "MLUPS",
-                "h2d_bytes_per_step": round(mesh_bytes / e2e_steps, 2),
-                "d2h_bytes_per_step": round(24 / 8, 2)},
-        "gpu_launches": args.steps,
+        "e2e": ({"value": round(cells * e2e_steps / (e2e_s * 1e6), 2), "unit": "MLUPS",
+                 "h2d_bytes_per_step": round(mesh_bytes / e2e_steps, 2),
+                 "d2h_bytes_per_step": round(24 / 8, 2)} if e2e_s else None),
+        "gpu_launches": launches,
         "clocks": results["f16"]["clocks"],
     }
-    line["storage_sweep"]["f16_over_f32"] = round(line["storage_sweep"]["f16"]["mlups"] /
-                                                  line["storage_sweep"]["f32"]["mlups"], 3)
+    if "f32" in line["storage_sweep"]:
+        line["storage_sweep"]["f16_over_f32"] = round(line["storage_sweep"]["f16"]["mlups"] /
+                                                      line["storage_sweep"]["f32"]["mlups"], 3)
     if world == 1 and args.cpu_steps > 0:
         flags = grid.flags.copy()
         cmlups, cdt = cpu_baseline(flags, args.cpu_steps, os.cpu_count() or 1)

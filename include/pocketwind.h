@@ -200,6 +200,12 @@ PW_API int pw_domain_buffers(pw_domain *dom, void **macros, void **flags, void *
 /* Time count steps on the domain's stream with CUDA events; *ms receives the
  * elapsed device time. */
 PW_API int pw_time_steps(pw_domain *dom, uint64_t count, float *ms);
+/* Queue `count` steps (no graphs) with CUDA events around each launch class and
+   sum their device times: kernel_ms[0] the plain-cell kernel, [1] its seam-row
+   variant (odd steps), [2] the edge-cell kernel.  Outside the fast build's
+   one-cell-per-thread path the whole step counts as [0].  No counterpart in the
+   reference (a measurement aid). */
+PW_API int pw_profile_steps(pw_domain *dom, uint64_t count, float kernel_ms[3]);
 
 /* ---------------------------------------------------------------- tracers */
 

@@ -78,6 +78,7 @@ SIGNATURES = {
     "pw_inject_nan": (_int, [_vp]),
     "pw_domain_buffers": (_int, [_vp, _PP, _PP, _PP]),
     "pw_time_steps": (_int, [_vp, _u64, C.POINTER(C.c_float)]),
+    "pw_profile_steps": (_int, [_vp, _u64, C.POINTER(C.c_float)]),
     "pw_particles_create": (_int, [_vp, _vp, _u32, _u32, _vp, _vp, _PP]),
     "pw_particles_update": (_int, [_vp, _f32]),
     "pw_particles_read": (_int, [_vp, _vp]),

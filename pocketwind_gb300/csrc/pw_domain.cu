@@ -11,6 +11,7 @@
 // steps without ramping are replayed from captured CUDA graphs.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -655,6 +656,46 @@ int pw_domain_buffers(pw_domain *d, void **macros, void **flags, void **stream) 
   if (macros) *macros = d->macros;
   if (flags) *flags = d->flags;
   if (stream) *stream = d->stream;
+  return PW_OK;
+}
+
+int pw_profile_steps(pw_domain *d, uint64_t count, float kernel_ms[3]) {
+  if (!alive(d) || !kernel_ms) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  kernel_ms[0] = kernel_ms[1] = kernel_ms[2] = 0.0f;
+  constexpr int kBatch = 32;
+  cudaEvent_t ev[kBatch][6];
+  int made = 0;
+  cudaError_t e = cudaSuccess;
+  for (; made < kBatch * 6 && e == cudaSuccess; made++) e = cudaEventCreate(&ev[made / 6][made % 6]);
+  uint64_t k = 0;
+  while (e == cudaSuccess && k < count) {
+    const int n = (int)std::min<uint64_t>(kBatch, count - k);
+    for (int b = 0; b < n; b++) {
+      const uint64_t step = d->steps + 1;
+      pw::StepParams p = params_for(d, step, ramp_speed(d, step), 0);
+      const bool odd = (step & 1) != 0;
+      if (d->split) {
+        pwfast::launch_step_split(p, d->desc.storage, d->desc.op, d->desc.les, odd, d->plain_grid, d->edges,
+                                  d->edge_count, d->stream, ev[b]);
+      } else {
+        cudaEventRecord(ev[b][0], d->stream);
+        enqueue_step(d, step, ramp_speed(d, step), 0);
+        for (int m = 1; m < 6; m++) cudaEventRecord(ev[b][m], d->stream);
+      }
+      d->steps++;
+    }
+    e = cudaEventSynchronize(ev[n - 1][5]);
+    for (int b = 0; b < n && e == cudaSuccess; b++) {
+      for (int c = 0; c < 3 && e == cudaSuccess; c++) {
+        float t = 0.0f;
+        e = cudaEventElapsedTime(&t, ev[b][2 * c], ev[b][2 * c + 1]);
+        kernel_ms[c] += t;
+      }
+    }
+    k += (uint64_t)n;
+  }
+  for (int m = 0; m < made; m++) cudaEventDestroy(ev[m / 6][m % 6]);
+  if (e != cudaSuccess) return cuda_status(e, "pw_profile_steps");
   return PW_OK;
 }
 

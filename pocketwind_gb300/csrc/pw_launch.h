@@ -34,9 +34,11 @@
 PW_DECLARE_LAUNCHERS(pwfast)
 namespace pwfast {
 // The fast build's split step: plain cells over plain_grid (the cell grid),
-// then the listed edge cells, whose blocks own the force partials.
+// then the listed edge cells, whose blocks own the force partials.  With ev
+// (6 events) it records around the plain kernel (0, 1), the seam-row kernel
+// (2, 3) and the edge kernel (4, 5).
 void launch_step_split(const pw::StepParams &p, int storage, int op, int les, bool odd, dim3 plain_grid,
-                       const uint32_t *list, uint32_t count, cudaStream_t s);
+                       const uint32_t *list, uint32_t count, cudaStream_t s, const cudaEvent_t *ev = nullptr);
 void launch_refresh_edges(const pw::StepParams &p, int odd_layout, int storage, const uint32_t *list,
                           uint32_t count, cudaStream_t s);
 }

@@ -1167,41 +1167,55 @@ void launch_step(const StepParams &p, int storage, int op, int les, bool odd, di
     default: { constexpr int ST = STORE_F32; CALL; break; } \
   }
 #if !PW_STRICT
+static inline void mark(const cudaEvent_t *ev, int k, cudaStream_t s) {
+  if (ev) cudaEventRecord(ev[k], s);
+}
 template <int ST, int OP, bool LES>
-static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *list, uint32_t count, cudaStream_t s) {
+static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *list, uint32_t count, cudaStream_t s,
+                        const cudaEvent_t *ev) {
   if (g.x && g.y && g.z) {
     const unsigned runs = (p.nx + 2 * BX - 1) / (2 * BX);  // 64-cell runs per row
     if (odd) {
       dim3 inner(runs, p.ny > 2u ? (p.ny - 2u + BY - 1u) / BY : 0u, p.nz > 2u ? p.nz - 2u : 0u);
+      mark(ev, 0, s);
       if (inner.y && inner.z) aa_step_fast<ST, OP, LES, true><<<inner, dim3(BX, BY), 0, s>>>(p);
+      mark(ev, 1, s);
+      mark(ev, 2, s);
       aa_step_seam<ST, OP, LES><<<dim3(g.x, seam_rows(p.ny, p.nz)), BX, 0, s>>>(p);
+      mark(ev, 3, s);
     } else {
+      mark(ev, 0, s);
       aa_step_fast<ST, OP, LES, false><<<dim3(runs, g.y, g.z), dim3(BX, BY), 0, s>>>(p);
+      mark(ev, 1, s);
+      mark(ev, 2, s);
+      mark(ev, 3, s);
     }
   }
+  mark(ev, 4, s);
   if (count) {
     unsigned blocks = (count + NTHREADS - 1) / NTHREADS;
     if (odd) aa_step_edges<ST, OP, LES, true><<<blocks, NTHREADS, 0, s>>>(p, list, count);
     else aa_step_edges<ST, OP, LES, false><<<blocks, NTHREADS, 0, s>>>(p, list, count);
   }
+  mark(ev, 5, s);
 }
 template <int ST>
 static void step_split2(const StepParams &p, int op, int les, bool odd, dim3 g, const uint32_t *list, uint32_t count,
-                        cudaStream_t s) {
+                        cudaStream_t s, const cudaEvent_t *ev) {
   if (op == OP_REG) {
-    if (les) step_split3<ST, OP_REG, true>(p, odd, g, list, count, s);
-    else step_split3<ST, OP_REG, false>(p, odd, g, list, count, s);
+    if (les) step_split3<ST, OP_REG, true>(p, odd, g, list, count, s, ev);
+    else step_split3<ST, OP_REG, false>(p, odd, g, list, count, s, ev);
   } else {
-    if (les) step_split3<ST, OP_TRT, true>(p, odd, g, list, count, s);
-    else step_split3<ST, OP_TRT, false>(p, odd, g, list, count, s);
+    if (les) step_split3<ST, OP_TRT, true>(p, odd, g, list, count, s, ev);
+    else step_split3<ST, OP_TRT, false>(p, odd, g, list, count, s, ev);
   }
 }
 void launch_step_split(const StepParams &p, int storage, int op, int les, bool odd, dim3 plain_grid,
-                       const uint32_t *list, uint32_t count, cudaStream_t s) {
+                       const uint32_t *list, uint32_t count, cudaStream_t s, const cudaEvent_t *ev) {
   switch (storage) {
-    case STORE_F16: step_split2<STORE_F16>(p, op, les, odd, plain_grid, list, count, s); break;
-    case STORE_BF16: step_split2<STORE_BF16>(p, op, les, odd, plain_grid, list, count, s); break;
-    default: step_split2<STORE_F32>(p, op, les, odd, plain_grid, list, count, s); break;
+    case STORE_F16: step_split2<STORE_F16>(p, op, les, odd, plain_grid, list, count, s, ev); break;
+    case STORE_BF16: step_split2<STORE_BF16>(p, op, les, odd, plain_grid, list, count, s, ev); break;
+    default: step_split2<STORE_F32>(p, op, les, odd, plain_grid, list, count, s, ev); break;
   }
 }
 #endif

@@ -124,6 +124,13 @@ class GpuSolver:
         _lib.check(_lib.load().pw_time_steps(self._live(), int(count), C.byref(ms)), "time_steps")
         return ms.value
 
+    def profile_steps(self, count: int) -> tuple:
+        """Summed device milliseconds of the plain-cell, seam-row and edge-cell
+        kernels over ``count`` steps (CUDA events around each launch)."""
+        ms = (C.c_float * 3)()
+        _lib.check(_lib.load().pw_profile_steps(self._live(), int(count), ms), "profile_steps")
+        return tuple(ms)
+
     # -------------------------------------------------------------- force
     def encode_force(self) -> None:
         _lib.check(_lib.load().pw_encode_force(self._live()), "encode_force")
