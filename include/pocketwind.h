@@ -72,9 +72,13 @@ typedef struct {
                            kernel on GB300); PW_KERNEL_TILE: whole x-rows staged through
                            shared memory by bulk copies, which needs nx * element bytes to
                            be a multiple of 16 (PW_ERR_INVALID otherwise) */
+  int lateral;          /* PW_LATERAL_PERIODIC (the reference: y and z wrap) or
+                           PW_LATERAL_FREE_SLIP (the y and z faces reflect specularly at
+                           the halfway plane; no counterpart in the reference) */
 } pw_domain_desc;
 
 enum { PW_KERNEL_AUTO = 0, PW_KERNEL_CELL = 1, PW_KERNEL_TILE = 2 };
+enum { PW_LATERAL_PERIODIC = 0, PW_LATERAL_FREE_SLIP = 1 };
 
 /* VoxelGrid statistics (src/geometry/voxel-grid.ts:7-15). */
 typedef struct {

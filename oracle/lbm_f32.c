@@ -15,6 +15,7 @@
  * product and sum is a separate IEEE binary32 operation, as in WGSL.
  */
 #include "pw_oracle.h"
+#include "slip.h"
 
 #include <math.h>
 #include <stdlib.h>
@@ -124,6 +125,7 @@ uint16_t ow_encode_bf16(float value, uint32_t i, uint32_t n) {
 
 struct ow_solver {
   uint32_t nx, ny, nz, cells;
+  int slip; /* free-slip faces, slip.h */
   float u_in, nu, cs_term, lambda;
   int les, op, walls, storage, threads;
   uint32_t *geometry;
@@ -376,7 +378,10 @@ static void cell_step(const ctx_t *c, uint32_t n) {
   float g[19], eq[19], post[19];
   g[0] = load_in(s, c->in, 0, n);
   for (int i = 1; i < 19; i++) {
-    if (has_wall(flag, i)) g[i] = wall_value(s, c->in, i, n, x, y, z, flag);
+    int k, oy, oz;
+    if (s->slip && slip_pull(s->slip, (int)s->ny, (int)s->nz, (int)y, (int)z, i, &k, &oy, &oz))
+      g[i] = load_in(s, c->in, k, idx_wrapped(s, x, y, z, -CX[i], oy, oz));
+    else if (has_wall(flag, i)) g[i] = wall_value(s, c->in, i, n, x, y, z, flag);
     else g[i] = load_in(s, c->in, i, idx_wrapped(s, x, y, z, -CX[i], -CY[i], -CZ[i]));
   }
   float rho_delta = 0.0f;
@@ -432,6 +437,8 @@ ow_solver *ow_create(uint32_t nx, uint32_t ny, uint32_t nz, float tau0, float u_
   return s;
 }
 
+void ow_set_lateral(ow_solver *s, int slip) { s->slip = slip; }
+
 void ow_destroy(ow_solver *s) {
   if (!s) return;
   free(s->geometry); free(s->boundary); free(s->state[0]); free(s->state[1]); free(s->macros);
@@ -473,6 +480,8 @@ void ow_force(const ow_solver *s, double out[3]) {
       uint32_t x = n % s->nx, y = (n / s->nx) % s->ny, z = n / (s->nx * s->ny);
       for (int i = 1; i < 19; i++) {
         if (!has_wall(flag, i)) continue;
+        int k, oy, oz;
+        if (s->slip && slip_pull(s->slip, (int)s->ny, (int)s->nz, (int)y, (int)z, i, &k, &oy, &oz)) continue;
         uint32_t nb = idx_wrapped(s, x, y, z, -CX[i], -CY[i], -CZ[i]);
         if ((s->geometry[nb] & 7u) != SOLID) continue;
         int j = opp(i);

@@ -8,6 +8,7 @@
  * IEEE binary64, the arithmetic of JavaScript numbers.
  */
 #include "pw_oracle.h"
+#include "slip.h"
 
 #include <math.h>
 #include <stdio.h>
@@ -188,6 +189,8 @@ typedef struct { uint32_t cell; int incoming; int type; double q; int64_t second
 
 struct oc_solver {
   uint32_t nx, ny, nz, cells;
+  int slip; /* free-slip faces, slip.h */
+  size_t links_cap;
   double tau0;
   int op, les, walls, threads;
   uint8_t *types;
@@ -224,6 +227,8 @@ static float f32_at(const uint32_t *geometry, size_t index) {
   return f;
 }
 
+static void build_sources(oc_solver *s, const uint32_t *geometry, size_t flags_len, char *err, size_t errlen);
+
 oc_solver *oc_create(uint32_t nx, uint32_t ny, uint32_t nz, double tau0, int op, int les,
                      const double body_force[3], int walls, const uint32_t *flags,
                      size_t flags_len, const double eq_state[4], const double *init_state,
@@ -249,7 +254,7 @@ oc_solver *oc_create(uint32_t nx, uint32_t ny, uint32_t nz, double tau0, int op,
   s->current = (double *)calloc(cells * 19, sizeof(double));
   s->next = (double *)calloc(cells * 19, sizeof(double));
   s->links = (wall_link *)malloc(sizeof(wall_link) * 64);
-  size_t cap = 64;
+  s->links_cap = 64;
   double rest[4] = {1, 0, 0, 0};
   const double *eqs = eq_state ? eq_state : rest;
   int bad = valid_state(eqs);
@@ -277,11 +282,29 @@ oc_solver *oc_create(uint32_t nx, uint32_t ny, uint32_t nz, double tau0, int op,
   memcpy(s->next, s->current, cells * 19 * sizeof(double));
   /* buildSources, cpu-solver.ts:144-197 */
   const uint32_t *geometry = walls == 1 ? flags : NULL;
+  build_sources(s, geometry, flags_len, err, errlen);
+  if (err && err[0]) { oc_destroy(s); return NULL; }
+  return s;
+#undef FAIL
+}
+
+/* buildSources (cpu-solver.ts:144-197), with free-slip faces (slip.h) */
+static void build_sources(oc_solver *s, const uint32_t *geometry, size_t flags_len, char *err, size_t errlen) {
+  size_t cells = s->cells;
+  if (err && errlen) err[0] = 0;
+  s->nlinks = 0;
   for (size_t cell = 0; cell < cells; cell++) {
     s->first_link[cell] = (int32_t)s->nlinks;
     if (s->types[cell] != FLUID) continue;
     int rank = 0;
+    uint32_t cx, cy, cz;
+    coords(s, (uint32_t)cell, &cx, &cy, &cz);
     for (int i = 0; i < 19; i++) {
+      int k, oy, oz;
+      if (s->slip && slip_pull(s->slip, (int)s->ny, (int)s->nz, (int)cy, (int)cz, i, &k, &oy, &oz)) {
+        s->sources[(size_t)i * cells + cell] = (int32_t)((size_t)k * cells + wrapped(s, (uint32_t)cell, -CX[i], oy, oz));
+        continue;
+      }
       uint32_t nb = wrapped(s, (uint32_t)cell, -CX[i], -CY[i], -CZ[i]);
       int type = s->types[nb];
       int wall = type >= SOLID && type <= FLOOR;
@@ -292,23 +315,29 @@ oc_solver *oc_create(uint32_t nx, uint32_t ny, uint32_t nz, double tau0, int op,
         uint32_t base = geometry[cells + cell];
         if (base != NO_Q) {
           size_t index = 2 * cells + base + (size_t)rank;
-          if (index >= flags_len) FAIL("Wall-link fraction is missing.");
+          if (index >= flags_len) { snprintf(err, errlen, "Wall-link fraction is missing."); return; }
           double fq = (double)f32_at(geometry, index);
-          if (!(fq > 0 && fq <= 1)) FAIL("Wall-link fraction must be in (0, 1].");
+          if (!(fq > 0 && fq <= 1)) { snprintf(err, errlen, "Wall-link fraction must be in (0, 1]."); return; }
           q = fq;
         }
       }
       uint32_t second = wrapped(s, (uint32_t)cell, CX[i], CY[i], CZ[i]);
       int short_link = q < HALFWAY_Q && s->types[second] == FLUID;
-      if (s->nlinks == cap) { cap *= 2; s->links = (wall_link *)realloc(s->links, cap * sizeof(wall_link)); }
+      if (s->nlinks == s->links_cap) {
+        s->links_cap *= 2;
+        s->links = (wall_link *)realloc(s->links, s->links_cap * sizeof(wall_link));
+      }
       wall_link L = {(uint32_t)cell, i, type, q, short_link ? (int64_t)second : -1};
       s->links[s->nlinks++] = L;
       rank += 1;
     }
   }
   s->first_link[cells] = (int32_t)s->nlinks;
-  return s;
-#undef FAIL
+}
+
+void oc_set_lateral(oc_solver *s, int slip, const uint32_t *flags, size_t flags_len, char *err, size_t errlen) {
+  s->slip = slip;
+  build_sources(s, s->walls == 1 ? flags : NULL, flags_len, err, errlen);
 }
 
 void oc_destroy(oc_solver *s) {

@@ -24,6 +24,7 @@ _lib = None
 OPERATORS = {"trt": 0, "reg": 1, "bgk": 2}
 WALLS = {"bb": 0, "bouzidi": 1}
 STORAGES = {"f32": 0, "f16": 1, "bf16": 2}
+LATERALS = {"periodic": 0, "free-slip": 3}  # slip.h: bit 0 y faces, bit 1 z faces
 
 
 def _p(a: Optional[np.ndarray]):
@@ -45,7 +46,8 @@ def lib():
             "ow_step": (None, [vp, f32, i32]), "ow_force": (None, [vp, vp]),
             "ow_populations": (None, [vp, vp]), "ow_populations_raw": (None, [vp, vp]),
             "ow_macros": (None, [vp, vp]), "ow_poke": (None, [vp, u32, u32, f32]),
-            "ow_params": (None, [vp, vp]),
+            "ow_params": (None, [vp, vp]), "ow_set_lateral": (None, [vp, i32]),
+            "oc_set_lateral": (None, [vp, i32, vp, sz, C.c_char_p, sz]),
             "oc_create": (vp, [u32, u32, u32, f64, i32, i32, vp, i32, vp, sz, vp, vp, i32, C.c_char_p, sz]),
             "oc_destroy": (None, [vp]), "oc_step": (None, [vp]),
             "oc_macroscopic": (None, [vp, u32, vp]), "oc_momentum_exchange": (None, [vp, vp]),
@@ -85,7 +87,7 @@ class Wgsl32:
     """Binary32 restatement of the reference's WGSL kernels with A/B ping-pong."""
 
     def __init__(self, nx, ny, nz, tau0, u_in, geometry, boundary=None, les=False, op="trt",
-                 walls="bb", storage="f32", threads=1, u_in_init=None):
+                 walls="bb", storage="f32", threads=1, u_in_init=None, lateral="periodic"):
         self.nx, self.ny, self.nz = nx, ny, nz
         self.cells = nx * ny * nz
         self.storage = storage
@@ -94,6 +96,8 @@ class Wgsl32:
         self._h = lib().ow_create(nx, ny, nz, np.float32(tau0), np.float32(u_in), int(les),
                                   OPERATORS[op], WALLS[walls], STORAGES[storage], _p(g), g.size,
                                   _p(b) if b.size else None, b.size, threads)
+        if LATERALS[lateral]:
+            lib().ow_set_lateral(self._h, LATERALS[lateral])
         if u_in_init is not None:
             self.reset(u_in_init)
 
@@ -142,7 +146,8 @@ class Cpu64:
     """Binary64 restatement of the reference's CpuSolver."""
 
     def __init__(self, layout, tau0, operator="trt", les=False, body_force=(0.0, 0.0, 0.0),
-                 walls="bb", flags=None, equilibrium_state=None, initial_state=None, threads=1):
+                 walls="bb", flags=None, equilibrium_state=None, initial_state=None, threads=1,
+                 lateral="periodic"):
         nx, ny, nz = layout
         self.layout = (nx, ny, nz)
         f = None if flags is None else np.ascontiguousarray(flags, dtype=np.uint32)
@@ -159,6 +164,10 @@ class Cpu64:
                                   threads, err, 256)
         if not self._h:
             raise ValueError(err.value.decode())
+        if LATERALS[lateral]:
+            lib().oc_set_lateral(self._h, LATERALS[lateral], _p(f), 0 if f is None else f.size, err, 256)
+            if err.value:
+                raise ValueError(err.value.decode())
         self.cells = lib().oc_cells(self._h)
 
     def __del__(self):

@@ -44,6 +44,8 @@ ow_solver *ow_create(uint32_t nx, uint32_t ny, uint32_t nz, float tau0, float u_
                      const uint32_t *geometry, size_t geometry_len,
                      const uint32_t *boundary, size_t nboundary, int threads);
 void ow_destroy(ow_solver *s);
+/* free-slip faces (bit 0: y, bit 1: z; slip.h), 0 = the reference's periodic wrap */
+void ow_set_lateral(ow_solver *s, int slip);
 void ow_reset(ow_solver *s, float u_in_init);
 /* one dispatch of stream_collide with the given inlet speed */
 void ow_step(ow_solver *s, float u_in, int write_macro);
@@ -69,6 +71,8 @@ oc_solver *oc_create(uint32_t nx, uint32_t ny, uint32_t nz, double tau0, int op,
                      const double eq_state[4], const double *init_state,
                      int threads, char *err, size_t errlen);
 void oc_destroy(oc_solver *s);
+/* free-slip faces as ow_set_lateral; rebuilds the pull sources from flags */
+void oc_set_lateral(oc_solver *s, int slip, const uint32_t *flags, size_t flags_len, char *err, size_t errlen);
 void oc_step(oc_solver *s);
 void oc_macroscopic(oc_solver *s, uint32_t cell, double out[4]);
 void oc_momentum_exchange(const oc_solver *s, double out[3]);

@@ -32,7 +32,7 @@ class DomainDesc(C.Structure):
     _fields_ = [("nx", C.c_uint32), ("ny", C.c_uint32), ("nz", C.c_uint32),
                 ("tau0", C.c_double), ("u_in", C.c_double), ("les", C.c_int), ("op", C.c_int),
                 ("walls", C.c_int), ("storage", C.c_int), ("ramp_steps", C.c_uint32), ("strict", C.c_int),
-                ("kernel", C.c_int)]
+                ("kernel", C.c_int), ("lateral", C.c_int)]
 
 
 class GridStats(C.Structure):

@@ -27,6 +27,14 @@ __host__ __device__ constexpr int cz_of(int i) {
          : (i == 6 || i == 10 || i == 12 || i == 15 || i == 17 ? -1 : 0);
 }
 __host__ __device__ constexpr int opp_of(int i) { return i == 0 ? 0 : ((i & 1) ? i + 1 : i - 1); }
+__host__ __device__ constexpr int dir_of(int cx, int cy, int cz, int k = 0) {
+  return k == 19 ? -1 : (cx_of(k) == cx && cy_of(k) == cy && cz_of(k) == cz ? k : dir_of(cx, cy, cz, k + 1));
+}
+// Direction i with its y (or z, or both) velocity component reversed: the
+// specular reflection at a free-slip face.
+__host__ __device__ constexpr int mirror_y(int i) { return dir_of(cx_of(i), -cy_of(i), cz_of(i)); }
+__host__ __device__ constexpr int mirror_z(int i) { return dir_of(cx_of(i), cy_of(i), -cz_of(i)); }
+__host__ __device__ constexpr int mirror_yz(int i) { return dir_of(cx_of(i), -cy_of(i), -cz_of(i)); }
 // binary32 weights, each 1/3, 1/18 or 1/36 rounded once (WGSL const-expression).
 __host__ __device__ constexpr float w_of(int i) {
   return i == 0 ? 0.333333343267440796f : (i < 7 ? 0.0555555559694766998f : 0.0277777779847383499f);
@@ -148,6 +156,7 @@ struct StepParams {
   float nu, cs_term, lambda;
   float tau0, omega_plus, omega_minus;  // binary32 constants of the LES-free operator
   int write_macro;
+  uint32_t slip;           // free-slip faces: bit 0 the y faces, bit 1 the z faces (0: periodic)
   // Plain cells (no periodic wrap in reach): direction i is loaded from element
   // n + ld[i] and stored to element n + st[i] of f, offsets for this step's parity.
   uint32_t ld[19];

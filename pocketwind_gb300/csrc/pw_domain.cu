@@ -104,6 +104,23 @@ __global__ void edge_write_kernel(const uint32_t *flags, const uint32_t *special
   if (pred) list[warp_base[threadIdx.x >> 5] + __popc(ballot & ((1u << lane) - 1u))] = n;
 }
 
+// Free-slip faces reflect instead of wrapping, so a wall link whose pull source
+// lies beyond one (a wall reached through the periodic wrap) does not exist.
+__global__ void clear_slip_links_kernel(uint32_t *flags, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t slip,
+                                        size_t cells) {
+  const size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= cells) return;
+  uint32_t f = flags[n];
+  if ((f >> 3) == 0u) return;
+  const uint32_t y = (uint32_t)((n / nx) % ny), z = (uint32_t)(n / ((size_t)nx * ny));
+  for (int i = 1; i < 19; i++) {
+    const int sy = (int)y - pw::cy_of(i), sz = (int)z - pw::cz_of(i);
+    const bool cross = ((slip & 1u) && (sy < 0 || sy >= (int)ny)) || ((slip & 2u) && (sz < 0 || sz >= (int)nz));
+    if (cross) f &= ~(1u << (3 + i));
+  }
+  flags[n] = f;
+}
+
 __global__ void first_fluid_kernel(const uint32_t *flags, size_t cells, unsigned long long *out) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < cells && (flags[i] & 7u) == pw::FLUID) atomicMin(out, (unsigned long long)i);
@@ -160,6 +177,7 @@ struct pw_domain {
   uint64_t force_step = 0;
   float u_in = 0, nu = 0, cs_term = 0, lambda = 0, tau0 = 0, om_p = 0, om_m = 0;
   dim3 grid;
+  uint32_t slip = 0;              // free-slip faces (bit 0 y, bit 1 z)
   bool split = false;             // fast build, one cell per thread: plain kernel + edge list
   uint32_t *edges = nullptr;      // edge cells in ascending order
   uint32_t edge_count = 0;
@@ -177,7 +195,7 @@ void domain_dims(const pw_domain *d, uint32_t *nx, uint32_t *ny, uint32_t *nz) {
   *nx = d->nx; *ny = d->ny; *nz = d->nz;
 }
 DomainView domain_view(const pw_domain *d) {
-  return DomainView{d->f, d->flags, d->nx, d->ny, d->nz, d->stride, d->steps, d->desc.storage, d->stream};
+  return DomainView{d->f, d->flags, d->nx, d->ny, d->nz, d->stride, d->steps, d->desc.storage, d->stream, d->slip};
 }
 }  // namespace pwhost
 
@@ -200,6 +218,7 @@ pw::StepParams params_for(const pw_domain *d, uint64_t step, float u_in, int wri
   p.nu = d->nu; p.cs_term = d->cs_term; p.lambda = d->lambda;
   p.tau0 = d->tau0; p.omega_plus = d->om_p; p.omega_minus = d->om_m;
   p.write_macro = write_macro;
+  p.slip = d->slip;
   // Per-direction element offsets of the plain cells.  Even steps read slot i
   // and write slot opp(j) of the cell itself; odd steps read slot opp(i) of
   // n - c_i and write slot j of n + c_j.  Every offset is non-negative
@@ -349,6 +368,14 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
   }
   if (desc->storage < 0 || desc->storage > 2) { set_error("Unknown population storage."); return PW_ERR_INVALID; }
   if (desc->kernel < PW_KERNEL_AUTO || desc->kernel > PW_KERNEL_TILE) { set_error("Unknown kernel choice."); return PW_ERR_INVALID; }
+  if (desc->lateral != PW_LATERAL_PERIODIC && desc->lateral != PW_LATERAL_FREE_SLIP) {
+    set_error("Unknown lateral boundary.");
+    return PW_ERR_INVALID;
+  }
+  if (desc->lateral == PW_LATERAL_FREE_SLIP && desc->kernel == PW_KERNEL_TILE) {
+    set_error("PW_KERNEL_TILE supports periodic lateral faces only.");
+    return PW_ERR_INVALID;
+  }
   if (desc->op != PW_OP_TRT && desc->op != PW_OP_REG) { set_error("Unknown collision operator."); return PW_ERR_INVALID; }
   if (desc->walls != PW_WALLS_BB) {
     set_error("Interpolated (Bouzidi) walls are not available in the in-place kernel; use halfway bounce-back.");
@@ -374,6 +401,7 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
   d->cells = cells;
   d->stride = (uint32_t)((cells + 63) / 64 * 64);
   d->esize = desc->storage == PW_STORE_F32 ? 4 : 2;
+  d->slip = desc->lateral == PW_LATERAL_FREE_SLIP ? 3u : 0u;
   d->u_in = uin;
   d->nu = nu;
   d->cs_term = (float)(18.0 * 1.4142135623730951 * (0.1 * 0.1));
@@ -446,6 +474,9 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
   cudaMemsetAsync(d->plane[0], 0, plane_n * sizeof(float4), s);
   cudaMemsetAsync(d->plane[1], 0, plane_n * sizeof(float4), s);
   cudaMemsetAsync(d->status_dev, 0, 16, s);
+  if (d->slip)
+    clear_slip_links_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(d->flags, d->nx, d->ny, d->nz, d->slip,
+                                                                           cells);
   special_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(d->flags, cells, d->special);
   cudaMemcpyAsync(ff, &none, 8, cudaMemcpyHostToDevice, s);
   first_fluid_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(d->flags, cells, ff);

@@ -30,6 +30,7 @@ struct DomainView {
   uint64_t steps;
   int storage;
   cudaStream_t stream;
+  uint32_t slip;  // free-slip faces (bit 0 y, bit 1 z)
 };
 DomainView domain_view(const pw_domain *d);
 

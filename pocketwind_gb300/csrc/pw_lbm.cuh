@@ -445,9 +445,30 @@ struct Nbr {
   uint32_t xm, x, xp;     // x - 1, x, x + 1 (periodic)
   uint32_t ym, y, yp;     // row offsets: (y-1)*nx, y*nx, (y+1)*nx
   uint32_t zm, z, zp;     // plane offsets
+  bool sym, syp, szm, szp;  // the -y / +y / -z / +z neighbour lies beyond a free-slip face
   __device__ __forceinline__ uint32_t at(int dx, int dy, int dz) const {
     return (dx < 0 ? xm : (dx > 0 ? xp : x)) + (dy < 0 ? ym : (dy > 0 ? yp : y)) +
            (dz < 0 ? zm : (dz > 0 ? zp : z));
+  }
+  // Odd steps push P(j, n) into slot j of n + c_j; across a free-slip face the
+  // population reflects: slot mirror(j) of the in-plane neighbour.  This is also
+  // where P(j, n) sits after an odd step (the readout map).
+  __device__ __forceinline__ uint32_t push(int j, uint32_t stride) const {
+    const int cy = cy_of(j), cz = cz_of(j);
+    const bool ry = (cy > 0 && syp) || (cy < 0 && sym);
+    const bool rz = (cz > 0 && szp) || (cz < 0 && szm);
+    const int k = ry ? (rz ? mirror_yz(j) : mirror_y(j)) : (rz ? mirror_z(j) : j);
+    return (uint32_t)k * stride + at(cx_of(j), ry ? 0 : cy, rz ? 0 : cz);
+  }
+  // Odd steps pull direction i from slot opp(i) of n - c_i; across a free-slip
+  // face from slot opp(mirror(i)) of the in-plane neighbour, where that
+  // neighbour's even step left P(mirror(i)).
+  __device__ __forceinline__ uint32_t pull(int i, uint32_t stride) const {
+    const int cy = -cy_of(i), cz = -cz_of(i);
+    const bool ry = (cy > 0 && syp) || (cy < 0 && sym);
+    const bool rz = (cz > 0 && szp) || (cz < 0 && szm);
+    const int k = ry ? (rz ? mirror_yz(i) : mirror_y(i)) : (rz ? mirror_z(i) : i);
+    return (uint32_t)opp_of(k) * stride + at(-cx_of(i), ry ? 0 : cy, rz ? 0 : cz);
   }
 };
 
@@ -463,13 +484,17 @@ __device__ __forceinline__ Nbr make_nbr(const StepParams &p, uint32_t x, uint32_
   b.z = z * plane;
   b.zm = (z == 0 ? p.nz - 1 : z - 1) * plane;
   b.zp = (z + 1 == p.nz ? 0 : z + 1) * plane;
+  b.sym = (p.slip & 1u) && y == 0;
+  b.syp = (p.slip & 1u) && y + 1 == p.ny;
+  b.szm = (p.slip & 2u) && z == 0;
+  b.szp = (p.slip & 2u) && z + 1 == p.nz;
   return b;
 }
 
 // Location of P(j, n) after a step of the given parity (the readout map).
 template <bool ODD_LAYOUT>
 __device__ __forceinline__ uint32_t slot_of(const Nbr &b, int j, uint32_t stride, uint32_t n) {
-  if (ODD_LAYOUT) return (uint32_t)j * stride + b.at(cx_of(j), cy_of(j), cz_of(j));
+  if (ODD_LAYOUT) return b.push(j, stride);
   return (uint32_t)opp_of(j) * stride + n;
 }
 
@@ -545,7 +570,7 @@ __device__ __forceinline__ void general_cell(const StepParams &p, uint32_t x, ui
 #pragma unroll
     for (int i = 0; i < 19; i++) {
       uint32_t src;
-      if (ODD) src = (uint32_t)opp_of(i) * S_ + b.at(-cx_of(i), -cy_of(i), -cz_of(i));
+      if (ODD) src = b.pull(i, S_);
       else src = (uint32_t)i * S_ + n;
       if (i > 0 && (flag & (1u << (3 + i)))) {  // wall link i: the slot nobody rewrites this step
         if (ODD) src = (uint32_t)i * S_ + n;
@@ -575,7 +600,7 @@ __device__ __forceinline__ void general_cell(const StepParams &p, uint32_t x, ui
 #pragma unroll
   for (int j = 0; j < 19; j++) {
     uint32_t dst;
-    if (ODD) dst = (uint32_t)j * S_ + b.at(cx_of(j), cy_of(j), cz_of(j));
+    if (ODD) dst = b.push(j, S_);
     else dst = (uint32_t)opp_of(j) * S_ + n;
     f[dst] = code[j];
   }
@@ -671,10 +696,8 @@ __device__ __forceinline__ void plain_cell(const StepParams &p, uint32_t n, uint
   }
 }
 
-// An EQ cell without wall links (the inlet and outlet planes), in the plain
-// kernels so that its stores share sectors with its row's plain cells:
-// stream_collide.wgsl:102-107 as in general_cell.  Odd steps store to n + c_j,
-// which wraps in x on the faces.
+// An EQ cell without wall links on a seam row (odd steps): stream_collide.wgsl:102-107
+// as in general_cell, stored through the seam kernel's wrapped offsets st.
 template <int ST, bool ODD>
 __device__ __forceinline__ void eq_cell(const StepParams &p, uint32_t n, uint32_t x, uint32_t y, uint32_t z,
                                         const uint32_t *st) {
@@ -686,13 +709,10 @@ __device__ __forceinline__ void eq_cell(const StepParams &p, uint32_t n, uint32_
     const float4 u = p.plane_in[y + p.ny * z];
     vx = u.x; vy = u.y; vz = u.z;
   }
-  const uint32_t xm = x == 0u ? p.nx : 0u, xp = x + 1u == p.nx ? 0u - p.nx : 0u;
   const uint32_t nk = n * 0x9e3779b9u;
 #pragma unroll
-  for (int j = 0; j < 19; j++) {
-    const uint32_t o = st[j] + (ODD ? (cx_of(j) < 0 ? xm : (cx_of(j) > 0 ? xp : 0u)) : 0u);
-    f[n + o] = S::encode_fast(geq_ref(j, 0.0f, vx, vy, vz) * S::kScale, dither_mul(j), nk);
-  }
+  for (int j = 0; j < 19; j++)
+    f[n + st[j]] = S::encode_fast(geq_ref(j, 0.0f, vx, vy, vz) * S::kScale, dither_mul(j), nk);
   if (p.write_macro) p.macros[n] = make_float4(1.0f + 0.0f, vx, vy, vz);
   if (x + 2 == p.nx) {
     const Nbr b = make_nbr(p, x, y, z);
@@ -838,15 +858,13 @@ __global__ void __launch_bounds__(BX) aa_step_seam(StepParams p) {
   if (x >= p.nx) return;
   const bool special = (__ldg(&p.special[n >> 5]) >> (n & 31u)) & 1u;
   if (special ? __ldg(&p.flags[n]) != EQ : !is_plain_position(x, p.nx)) return;
-  const uint32_t plane = p.nx * p.ny;
-  const uint32_t ym = y == 0u ? p.ny * p.nx : 0u, yp = y + 1u == p.ny ? 0u - p.ny * p.nx : 0u;
-  const uint32_t zm = z == 0u ? p.nz * plane : 0u, zp = z + 1u == p.nz ? 0u - p.nz * plane : 0u;
+  // offsets relative to n of the wrapped (or reflected, on free-slip faces) slots
+  const Nbr b = make_nbr(p, x, y, z);
   uint32_t ld[19], st[19];
 #pragma unroll
   for (int i = 0; i < 19; i++) {
-    // loads come from n - c_i, stores go to n + c_i
-    ld[i] = p.ld[i] + (cy_of(i) > 0 ? ym : (cy_of(i) < 0 ? yp : 0u)) + (cz_of(i) > 0 ? zm : (cz_of(i) < 0 ? zp : 0u));
-    st[i] = p.st[i] + (cy_of(i) > 0 ? yp : (cy_of(i) < 0 ? ym : 0u)) + (cz_of(i) > 0 ? zp : (cz_of(i) < 0 ? zm : 0u));
+    ld[i] = b.pull(i, p.stride) - n;
+    st[i] = b.push(i, p.stride) - n;
   }
   if (special) eq_cell<ST, true>(p, n, x, y, z, st);
   else plain_cell<ST, OP, LES, true>(p, n, x, y, z, ld, st);

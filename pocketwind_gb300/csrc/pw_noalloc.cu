@@ -109,6 +109,7 @@ int pw_read_populations_noalloc(pw_domain *dom, float *out) {
   p.flags = v.flags;
   p.nx = v.nx; p.ny = v.ny; p.nz = v.nz;
   p.stride = v.stride;
+  p.slip = v.slip;
   const int odd = (int)(v.steps & 1);
   const size_t cells = plane * v.nz;
   const uint32_t zc = (uint32_t)std::min<size_t>(v.nz, kScratchBytes / plane_bytes);

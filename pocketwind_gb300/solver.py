@@ -43,6 +43,7 @@ class SolverParams:
     ramp_steps: int = 0
     strict: bool = False
     kernel: str = "auto"  # "auto" or "cell" (one cell per thread), "tile" (x-rows staged in shared memory)
+    lateral: str = "periodic"  # or "free-slip": the y and z faces reflect (no counterpart in the reference)
 
 
 @dataclass
@@ -69,6 +70,8 @@ class GpuSolver:
             raise RangeError("Ramp steps must be a non-negative safe integer.")
         if params.operator not in OPERATORS or params.walls not in WALLS or params.precision not in PRECISIONS:
             raise RangeError("Unknown operator, wall treatment or precision.")
+        if params.lateral not in ("periodic", "free-slip") or params.kernel not in ("auto", "cell", "tile"):
+            raise RangeError("Unknown lateral boundary or kernel choice.")
         nx, ny, nz = (int(v) for v in layout)
         if (nx, ny, nz) != (grid.nx, grid.ny, grid.nz):
             raise RangeError("Geometry must match the solver layout and contain flags and q offsets.")
@@ -76,7 +79,8 @@ class GpuSolver:
         _lib.require_gpu()
         d = _lib.DomainDesc(nx, ny, nz, float(params.tau0), float(params.u_in), int(bool(params.les)),
                             OPERATORS[params.operator], WALLS[params.walls], PRECISIONS[params.precision],
-                            ramp, int(bool(params.strict)), {"auto": 0, "cell": 1, "tile": 2}[params.kernel])
+                            ramp, int(bool(params.strict)), {"auto": 0, "cell": 1, "tile": 2}[params.kernel],
+                            {"periodic": 0, "free-slip": 1}[params.lateral])
         out = C.c_void_p()
         rc = L.pw_domain_create(C.byref(d), grid._handle.ptr, C.byref(out))
         if rc == _lib.PW_ERR_OOM:

@@ -35,12 +35,12 @@ def _pw():
 
 
 def make_solver(geometry, boundary, layout=LAYOUT, tau0=0.8, u_in=0.06, les=False, op="trt",
-                precision="f32", strict=False, ramp=0, kernel="auto"):
+                precision="f32", strict=False, ramp=0, kernel="auto", lateral="periodic"):
     G, S = _pw()
     grid = G.grid_from_arrays(layout, geometry, boundary)
     s = S.GpuSolver.create(layout, grid, S.SolverParams(tau0=tau0, u_in=u_in, les=les, operator=op,
                                                          precision=precision, strict=strict, ramp_steps=ramp,
-                                                         kernel=kernel))
+                                                         kernel=kernel, lateral=lateral))
     assert not isinstance(s, Exception)
     return s
 
@@ -371,3 +371,71 @@ def test_staged_rows_equal_cell_kernel_on_vehicle(precision, strict):
         a.step(n, True)
         b.step(n, True)
         _pair_equal(a, b, precision, exact=strict)
+
+
+# ---------------------------------------------------------------- free-slip lateral faces
+SLIP_CHECKPOINTS = [1, 10, 25, 50, 100]
+
+
+@pytest.mark.parametrize("precision", ["f32", "f16"])
+def test_free_slip_strict_is_bit_exact(precision):
+    """The free-slip option (no reference counterpart) against its binary32 restatement:
+    the y and z faces reflect, wall links through the wrap are dropped, and the
+    AA readout follows the reflected slots on odd steps."""
+    geometry, boundary = blob_grid("bb")
+    gpu = make_solver(geometry, boundary, precision=precision, strict=True, lateral="free-slip")
+    ref = O.Wgsl32(32, 32, 32, 0.8, 0.06, geometry, boundary, storage=precision, threads=THREADS,
+                   lateral="free-slip")
+    view = np.uint32 if precision == "f32" else np.uint16
+    done = 0
+    for cp in SLIP_CHECKPOINTS:
+        while done < cp:
+            last = done == cp - 1
+            gpu.step(1, last)
+            ref.step(0.06, last)
+            done += 1
+        assert np.array_equal(gpu.populations_raw().view(view), ref.populations_raw().view(view)), cp
+        assert np.array_equal(gpu.macros().reshape(-1).view(np.uint32), ref.macros().view(np.uint32)), cp
+        gpu.encode_force()
+        f = gpu.read_force()
+        assert np.allclose([f.fx, f.fy, f.fz], ref.force(), rtol=1e-12, atol=1e-15), cp
+
+
+@pytest.mark.parametrize("op,les", CONFIGS)
+def test_free_slip_fast_matches_fp64_reference(op, les):
+    geometry, boundary = blob_grid("bb")
+    gpu = make_solver(geometry, boundary, les=les, op=op, lateral="free-slip")
+    cpu = O.Cpu64(LAYOUT, 0.8, operator=op, les=les, flags=geometry[:CELLS],
+                  equilibrium_state=(1, (0.06, 0, 0)), threads=THREADS, lateral="free-slip")
+    done = 0
+    for cp in SLIP_CHECKPOINTS:
+        while done < cp:
+            gpu.step(1, done == cp - 1)
+            cpu.step()
+            done += 1
+        assert norm_err(gpu.populations(), cpu.populations) < 1e-5, cp
+        assert norm_err(gpu.macros()[:, 1:].astype(np.float64), cpu.macros()[:, 1:]) < 1e-5, cp
+
+
+def test_free_slip_write_read_round_trip_and_mass():
+    """Write-in and readout follow the reflected slots in both layouts; a closed
+    free-slip channel conserves mass."""
+    geometry = np.concatenate([np.zeros(CELLS, np.uint32), np.full(CELLS, NO_Q, np.uint32)])
+    gpu = make_solver(geometry, np.zeros(0, np.uint32), lateral="free-slip")
+    rng = np.random.default_rng(5)
+    for parity_steps in (3, 2):
+        gpu.step(parity_steps)
+        g = (rng.standard_normal(19 * CELLS) * 1e-3).astype(np.float32)
+        gpu.write_populations(g)
+        assert np.array_equal(gpu.populations(), g)
+    m0 = gpu.totals()[0]
+    gpu.step(40)
+    assert abs(gpu.totals()[0] - m0) < 1e-9 * CELLS
+
+
+def test_free_slip_rejects_the_staged_kernel():
+    geometry, boundary = blob_grid("bb")
+    G, S = _pw()
+    grid = G.grid_from_arrays(LAYOUT, geometry, boundary)
+    with pytest.raises(S.RangeError):
+        S.GpuSolver.create(LAYOUT, grid, S.SolverParams(tau0=0.8, u_in=0.06, kernel="tile", lateral="free-slip"))

@@ -535,3 +535,82 @@ def test_poiseuille_reg(tau0):
     r = run_poiseuille(tau0, "reg")
     assert abs(r["max_speed_err"]) < 1 and r["profile_err"] < 1
     assert close(r["force"][0], r["expected"], 8)
+
+
+# ---------------------------------------------------------------- free-slip faces
+# The project's lateral option (no reference counterpart): the y and z faces
+# reflect specularly at the halfway plane.  Its oracle is pinned here by the
+# invariants such a boundary must keep, in binary64 and binary32.
+
+def test_free_slip_keeps_a_tangential_uniform_flow_exactly():
+    c = O.Cpu64((8, 6, 5), 0.8, equilibrium_state=(1.0, (0.05, 0.0, 0.0)), lateral="free-slip")
+    c.step(5)
+    m = c.macros()
+    assert np.abs(m[:, 0] - 1).max() < 1e-15 and np.abs(m[:, 1] - 0.05).max() < 1e-15
+    assert np.abs(m[:, 2:]).max() < 1e-16
+
+
+def test_free_slip_conserves_mass_and_tangential_momentum():
+    """A normal velocity is reversed at the faces: mass and the x momentum of a
+    closed free-slip channel (periodic x) are conserved exactly; the y and z
+    momentum are not."""
+    layout = (6, 5, 4)
+    rng = np.random.default_rng(3)
+    init = np.zeros((6 * 5 * 4, 4))
+    init[:, 0] = 1 + 0.01 * rng.standard_normal(len(init))
+    init[:, 1:] = 0.02 * rng.standard_normal((len(init), 3))
+    c = O.Cpu64(layout, 0.7, initial_state=init, lateral="free-slip")
+    m0 = c.macros()
+    mass0, jx0 = m0[:, 0].sum(), (m0[:, 0] * m0[:, 1]).sum()
+    c.step(20)
+    m = c.macros()
+    assert abs(m[:, 0].sum() - mass0) < 1e-12
+    assert abs((m[:, 0] * m[:, 1]).sum() - jx0) < 1e-12
+
+
+@pytest.mark.parametrize("i", [k for k in range(1, 19) if C[k][1] != 0 or C[k][2] != 0])
+def test_free_slip_reflects_per_direction(i):
+    """A 0.001 deviation leaving through a slip face (the cell on that face,
+    population i pointing out of it) arrives after one step at the in-plane
+    neighbour x + c_x (z + c_z for a y face, and so on) with the normal
+    components reversed: density 1.001 and velocity mirror(c_i) * 0.001 / 1.001
+    there, in both restatements.  Mirrors test_periodic_pull_per_direction."""
+    n = 5
+    cx, cy, cz = C[i]
+    x0 = 2
+    y0 = 0 if cy < 0 else (n - 1 if cy > 0 else 2)
+    z0 = 0 if cz < 0 else (n - 1 if cz > 0 else 2)
+    src = x0 + n * (y0 + n * z0)
+    dest = (x0 + cx) % n + n * (y0 + n * z0)
+    mirrored = (cx, -cy, -cz)
+    s = O.Cpu64((n, n, n), 0.8, lateral="free-slip")
+    s.populations[i * s.cells + src] = 0.001
+    s.step()
+    geometry = np.concatenate([np.zeros(125, np.uint32), np.full(125, NO_Q, np.uint32)])
+    w = O.Wgsl32(n, n, n, 0.8, 0.0, geometry, lateral="free-slip")
+    w.poke(i, src, 0.001)
+    w.step(0.0, True)
+    mac = w.macros().reshape(125, 4)
+    for cell in range(125):
+        rho, u = s.macroscopic(cell)
+        ex = 0.001 if cell == dest else 0.0
+        assert close(rho, 1 + ex, 14), cell
+        for a in range(3):
+            assert close(u[a], mirrored[a] * ex / (1 + ex), 14)
+        assert abs(mac[cell, 0] - (1 + ex)) < 1e-6
+        for a in range(3):
+            assert abs(mac[cell, 1 + a] - mirrored[a] * ex / (1 + ex)) < 1e-7
+
+
+def test_free_slip_binary32_tracks_binary64():
+    from tests.shapes import blob_grid
+    geometry, boundary = blob_grid("bb")
+    cells = 32 ** 3
+    f = O.Wgsl32(32, 32, 32, 0.8, 0.06, geometry, boundary, threads=4, lateral="free-slip")
+    d = O.Cpu64((32, 32, 32), 0.8, flags=geometry[:cells], equilibrium_state=(1, (0.06, 0, 0)), threads=4,
+                lateral="free-slip")
+    for _ in range(30):
+        f.step(0.06)
+        d.step()
+    a, b = f.populations().astype(np.float64), d.populations
+    assert np.abs(a - b).max() / np.abs(b).max() < 1e-5
