@@ -24,6 +24,8 @@ roofline: the plain-cell kernels (the two-cell packed-FP32 kernel, and on odd
 cpu_baseline: the binary64 restatement of the reference's CpuSolver (the
           reference's CPU path; the TypeScript original cannot run here), on all
           host cores, over a bounded number of full-domain steps.
+accuracy: drag and field errors against that binary64 restatement: the sphere
+          at Re 100 (96x48x48, FP32) and the 128x64x64 vehicle in each storage.
 
 --impl reference runs only that CPU path and prints its own line.
 """
@@ -185,6 +187,59 @@ def run_ours(args, rank, world):
     return results, e2e_s, e2e_steps, body.positions.nbytes, cells, grid
 
 
+def accuracy_leg(steps, threads):
+    """Drag and field errors against the binary64 CpuSolver restatement on the same
+    voxel grids: the laminar sphere at Re 100 (96x48x48, FP32, TRT, free-slip
+    lateral faces, 4,000 steps, drag averaged over steps 3,001-4,000) and the
+    128x64x64 vehicle (REG + LES + wall model, floor) in each storage after
+    `steps` steps."""
+    import numpy as np
+    from oracle import oracle as O
+    from pocketwind_gb300 import cases, forces
+    from pocketwind_gb300.solver import GpuSolver
+    out = {}
+    c = cases.sphere_case("free-slip")
+    grid = c.grid()
+    s = GpuSolver.create(c.layout, grid, c.params("f32"))
+    fx, fy, fz = cases.mean_drag(cases.run_drag(s, c.steps), c.steps, c.average_steps)
+    s.destroy()
+    cpu = O.Cpu64(c.layout, c.tau0, flags=grid.flags, equilibrium_state=(1.0, (c.u_in, 0.0, 0.0)),
+                  threads=threads, lateral=c.lateral)
+    window = []
+    for k in range(8, c.steps + 1, 8):
+        cpu.step(8)
+        if k > c.steps - c.average_steps:
+            window.append(cpu.momentum_exchange()[0])
+    rfx = float(np.mean(window))
+    out["sphere_re100"] = {"grid": "96x48x48", "storage": "f32", "operator": "trt", "lateral": "free-slip",
+                           "steps": c.steps, "average_steps": c.average_steps, "fx": fx, "fx_fp64": rfx,
+                           "drag_rel_err": abs(fx - rfx) / abs(rfx),
+                           "cd": fx * forces.cd_per_lattice_force(grid.frontal_cells),
+                           "frontal_cells": grid.frontal_cells}
+    v = cases.vehicle_case(128)
+    grid = v.grid()
+    cpu = O.Cpu64(v.layout, v.tau0, operator="reg", les=True, flags=grid.flags,
+                  equilibrium_state=(1.0, (v.u_in, 0.0, 0.0)), threads=threads)
+    cpu.step(steps)
+    ref, fr = cpu.macros(), cpu.momentum_exchange()
+    fluid = (grid.flags & 7) == 0
+    per = {}
+    for precision in ("f32", "f16", "bf16"):
+        s = GpuSolver.create(v.layout, grid, v.params(precision))
+        s.step(steps, True)
+        m = s.macros().astype(np.float64)
+        s.encode_force()
+        f = s.read_force()
+        s.destroy()
+        per[precision] = {
+            "u_l2_rel": float(np.linalg.norm((m[:, 1:] - ref[:, 1:])[fluid]) / np.linalg.norm(ref[:, 1:][fluid])),
+            "rho_l2_rel": float(np.linalg.norm((m[:, 0] - ref[:, 0])[fluid]) /
+                                np.linalg.norm((ref[:, 0] - 1)[fluid])),
+            "drag_rel_err": abs(f.fx - fr[0]) / abs(fr[0])}
+    out["vehicle_128"] = {"grid": "128x64x64", "operator": "reg+les+wall model", "steps": steps, "storages": per}
+    return out
+
+
 def cell_classes(flags):
     """Cells updated per step by the plain-cell kernels (plain fluid with
     1 <= x <= nx-2, and EQ cells without wall links) and by the edge kernel."""
@@ -217,6 +272,8 @@ def main():
     ap.add_argument("--nx", type=int, default=512, help="profiling runs: the case at nx x nx/2 x nx/2")
     ap.add_argument("--only", default="f16,f32,bf16", help="profiling runs: storages to time (f16 first)")
     ap.add_argument("--no-e2e", action="store_true", help="profiling runs: skip the end-to-end leg")
+    ap.add_argument("--accuracy-steps", type=int, default=1000,
+                    help="vehicle steps of the accuracy leg against FP64 (0 skips the leg)")
     args = ap.parse_args()
     if args.nx != 512:
         set_size(args.nx)
@@ -315,6 +372,8 @@ def main():
     if "f32" in line["storage_sweep"]:
         line["storage_sweep"]["f16_over_f32"] = round(line["storage_sweep"]["f16"]["mlups"] /
                                                       line["storage_sweep"]["f32"]["mlups"], 3)
+    if world == 1 and args.accuracy_steps > 0:
+        line["accuracy"] = accuracy_leg(args.accuracy_steps, os.cpu_count() or 1)
     if world == 1 and args.cpu_steps > 0:
         flags = grid.flags.copy()
         cmlups, cdt = cpu_baseline(flags, args.cpu_steps, os.cpu_count() or 1)
