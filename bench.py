@@ -26,6 +26,9 @@ cpu_baseline: the binary64 restatement of the reference's CpuSolver (the
           host cores, over a bounded number of full-domain steps.
 accuracy: drag and field errors against that binary64 restatement: the sphere
           at Re 100 (96x48x48, FP32) and the 128x64x64 vehicle in each storage.
+batched_tunnels: 64 seeded tunnels of uneven size and Re, FP16 TRT, one
+          persistent launch per step from captured graphs, autotuned shape;
+          aggregate MLUPS and drag error against each tunnel alone in FP32.
 
 --impl reference runs only that CPU path and prints its own line.
 """
@@ -240,6 +243,65 @@ def accuracy_leg(steps, threads):
     return out
 
 
+def batch_leg(steps, sample_steps=200, count=64, peak=None):
+    """64 independent tunnels (sizes, bodies and Re from splitmix64 seed 1), FP16
+    storage, TRT, stepped as one batch: one persistent launch per step over all
+    members, replayed from captured 50-step graphs, launch shape from the
+    autotuner.  Aggregate MLUPS over `steps` steps, then each member's drag over
+    the last `sample_steps` steps against the same tunnel run alone in FP32."""
+    import numpy as np
+    from pocketwind_gb300 import cases, geometry, solver
+    from pocketwind_gb300.batch import Batch
+    tunnels = cases.batch_tunnels(count, 1)
+    grids = [geometry.voxelize(t.body, None, t.layout, False) for t in tunnels]
+
+    def make(i, precision):
+        t = tunnels[i]
+        return solver.GpuSolver.create(t.layout, grids[i], solver.SolverParams(
+            tau0=t.tau0, u_in=0.05, operator="trt", precision=precision))
+
+    members = [make(i, "f16") for i in range(count)]
+    batch = Batch(members)
+    tuning = batch.tune(8)
+    batch.reset()
+    ms = batch.time_steps(steps)
+    cells = batch.cells
+
+    def sampled(step, sols, every=8):
+        acc = np.zeros(len(sols))
+        for _ in range(sample_steps // every):
+            step(every)
+            for k, s in enumerate(sols):
+                s.encode_force()
+                acc[k] += s.read_force().fx
+        return acc / (sample_steps // every)
+
+    batch.reset()
+    batch.step(steps - sample_steps)
+    fx16 = sampled(batch.step, members)
+    batch.destroy()
+    for m in members:
+        m.destroy()
+    fx32 = np.zeros(count)
+    for i in range(count):
+        s = make(i, "f32")
+        s.step(steps - sample_steps)
+        fx32[i] = sampled(s.step, [s])[0]
+        s.destroy()
+    err = np.abs(fx16 - fx32) / np.abs(fx32)
+    mlups = cells * steps / (ms * 1e3)
+    out = {"domains": count, "cells": cells, "steps": steps, "storage": "f16", "operator": "trt",
+           "ms_per_step": round(ms / steps, 4), "mlups": round(mlups, 1),
+           "launches_per_step": 1, "graph_chunk_steps": 50,
+           "tuning": {"blocks": tuning.blocks, "rows_per_item": tuning.rows_per_item,
+                      "candidates": tuning.candidates},
+           "drag_rel_err_vs_solo_f32": {"median": float(np.median(err)), "p90": float(np.percentile(err, 90)),
+                                        "max": float(err.max()), "sample_steps": sample_steps}}
+    if peak:
+        out["hbm_frac"] = round(mlups * 1e6 * BYTES["f16"] / (peak * 1e9), 4)
+    return out
+
+
 def cell_classes(flags):
     """Cells updated per step by the plain-cell kernels (plain fluid with
     1 <= x <= nx-2, and EQ cells without wall links) and by the edge kernel."""
@@ -272,6 +334,8 @@ def main():
     ap.add_argument("--nx", type=int, default=512, help="profiling runs: the case at nx x nx/2 x nx/2")
     ap.add_argument("--only", default="f16,f32,bf16", help="profiling runs: storages to time (f16 first)")
     ap.add_argument("--no-e2e", action="store_true", help="profiling runs: skip the end-to-end leg")
+    ap.add_argument("--batch-steps", type=int, default=2000,
+                    help="steps of the 64-tunnel batched leg (0 skips the leg)")
     ap.add_argument("--accuracy-steps", type=int, default=1000,
                     help="vehicle steps of the accuracy leg against FP64 (0 skips the leg)")
     args = ap.parse_args()
@@ -372,6 +436,8 @@ def main():
     if "f32" in line["storage_sweep"]:
         line["storage_sweep"]["f16_over_f32"] = round(line["storage_sweep"]["f16"]["mlups"] /
                                                       line["storage_sweep"]["f32"]["mlups"], 3)
+    if world == 1 and args.batch_steps > 0:
+        line["batched_tunnels"] = batch_leg(args.batch_steps, peak=peak)
     if world == 1 and args.accuracy_steps > 0:
         line["accuracy"] = accuracy_leg(args.accuracy_steps, os.cpu_count() or 1)
     if world == 1 and args.cpu_steps > 0:

@@ -203,6 +203,31 @@ PW_API int pw_inject_nan(pw_domain *dom);
 PW_API int pw_domain_buffers(pw_domain *dom, void **macros, void **flags, void **stream);
 /* Time count steps on the domain's stream with CUDA events; *ms receives the
  * elapsed device time. */
+/* ---- batches: many independent domains stepped together (no reference counterpart;
+   the reference runs one solver at a time, src/app/solver-slot.ts) ----
+   Members are domains of the fast build's one-cell-per-thread path sharing
+   storage, operator and LES, with equal step counts and no ramp in progress.
+   Each batch step is one persistent launch over all members' work, replayed
+   from captured CUDA graphs; members keep their own force, macro and readout
+   calls, which wait for the batch's queued steps.  A member must not be
+   stepped on its own while it belongs to a batch. */
+typedef struct pw_batch pw_batch;
+typedef struct {
+  uint32_t blocks;         /* persistent grid chosen */
+  uint32_t rows_per_item;  /* plain rows per work item chosen */
+  float ms_per_step;       /* its measured time per step */
+  uint32_t candidates;     /* launch shapes timed */
+} pw_batch_tuning;
+PW_API int pw_batch_create(pw_domain *const *members, uint32_t count, pw_batch **out);
+PW_API void pw_batch_destroy(pw_batch *batch);
+PW_API int pw_batch_step(pw_batch *batch, uint64_t count, int write_macro_on_last);
+PW_API int pw_batch_time_steps(pw_batch *batch, uint64_t count, float *ms);
+/* Autotuner: times each candidate shape over trial_steps real steps (they
+   advance the members) and keeps the fastest. */
+PW_API int pw_batch_tune(pw_batch *batch, uint32_t trial_steps, pw_batch_tuning *out);
+/* pw_reset of every member; the batch starts again at step 0. */
+PW_API int pw_batch_reset(pw_batch *batch);
+
 PW_API int pw_time_steps(pw_domain *dom, uint64_t count, float *ms);
 /* Queue `count` steps (no graphs) with CUDA events around each launch class and
    sum their device times: kernel_ms[0] the plain-cell kernel, [1] its seam-row

@@ -79,6 +79,12 @@ SIGNATURES = {
     "pw_domain_buffers": (_int, [_vp, _PP, _PP, _PP]),
     "pw_time_steps": (_int, [_vp, _u64, C.POINTER(C.c_float)]),
     "pw_profile_steps": (_int, [_vp, _u64, C.POINTER(C.c_float)]),
+    "pw_batch_create": (_int, [C.POINTER(_vp), C.c_uint32, C.POINTER(_vp)]),
+    "pw_batch_destroy": (None, [_vp]),
+    "pw_batch_step": (_int, [_vp, _u64, _int]),
+    "pw_batch_time_steps": (_int, [_vp, _u64, C.POINTER(C.c_float)]),
+    "pw_batch_tune": (_int, [_vp, C.c_uint32, C.c_void_p]),
+    "pw_batch_reset": (_int, [_vp]),
     "pw_particles_create": (_int, [_vp, _vp, _u32, _u32, _vp, _vp, _PP]),
     "pw_particles_update": (_int, [_vp, _f32]),
     "pw_particles_read": (_int, [_vp, _vp]),

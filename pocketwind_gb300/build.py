@@ -30,6 +30,7 @@ UNITS = {
     "pw_tracers.cu": ["-fmad=false"],
     "pw_domain.cu": [],
     "pw_noalloc.cu": [],
+    "pw_batch.cu": [],
 }
 HEADERS = ["pw_common.cuh", "pw_lbm.cuh", "pw_lbm_tile.cuh", "pw_launch.h", "pw_internal.h"]
 

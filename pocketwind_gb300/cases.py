@@ -86,3 +86,70 @@ def run_drag(solver: GpuSolver, steps: int, every: int = forces.FORCE_EVERY_STEP
 
 def mean_drag(samples, steps: int, average_steps: int):
     return forces.averaged_forces(samples, steps, average_steps)
+
+
+# ---------------------------------------------------------------- batched tunnels
+BATCH_SIZES = ((64, 32, 32), (96, 48, 48), (128, 64, 64), (192, 96, 96))
+NU_MIN_LU = 1e-2  # the reference's lattice viscosity floor (src/lbm/units.ts:7,33)
+
+
+class SplitMix64:
+    """The splitmix64 generator (Steele, Lea and Flood, 2014): the seeded draws
+    of the batched-tunnel case."""
+
+    def __init__(self, seed: int):
+        self.state = seed & 0xFFFFFFFFFFFFFFFF
+
+    def next(self) -> int:
+        self.state = (self.state + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+        z = self.state
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+        return z ^ (z >> 31)
+
+    def uniform(self, lo: float = 0.0, hi: float = 1.0) -> float:
+        return lo + (hi - lo) * ((self.next() >> 11) * (1.0 / 9007199254740992.0))
+
+    def choice(self, n: int) -> int:
+        return min(n - 1, int(self.uniform() * n))
+
+
+@dataclass
+class Tunnel:
+    layout: tuple
+    shape: str
+    body: meshes.Mesh
+    re: float
+    tau0: float
+    length: float
+    params_note: dict
+
+
+def batch_tunnels(count: int = 64, seed: int = 1, u: float = forces.U_LU) -> List[Tunnel]:
+    """Independent tunnels of uneven size and Reynolds number: sizes drawn
+    uniformly from BATCH_SIZES, bodies a sphere, an ellipsoid (axis ratios
+    U[1, 3]) or a box yawed U[0, 30] degrees, body length nx/8 centred at x =
+    nx/4, Re U[20, 300] on that length, u = 0.05.  The lattice viscosity is
+    max(0.01, u L / Re), the reference's floor, which keeps tau0 >= 0.53."""
+    rng = SplitMix64(seed)
+    out = []
+    for _ in range(count):
+        nx, ny, nz = BATCH_SIZES[rng.choice(len(BATCH_SIZES))]
+        kind = ("sphere", "ellipsoid", "box")[rng.choice(3)]
+        re = rng.uniform(20.0, 300.0)
+        length = nx / 8
+        centre = (nx / 4, ny / 2, nz / 2)
+        note = {}
+        if kind == "sphere":
+            body = meshes.icosphere(centre, length / 2, 3)
+        elif kind == "ellipsoid":
+            ry, rz = rng.uniform(1.0, 3.0), rng.uniform(1.0, 3.0)
+            body = meshes.ellipsoid(centre, (length / 2, length / 2 / ry, length / 2 / rz), 3)
+            note = {"axis_ratios": (ry, rz)}
+        else:
+            yaw = rng.uniform(0.0, 30.0)
+            body = meshes.yawed_box(centre, (length, length / 2, length / 2), yaw)
+            note = {"yaw_deg": yaw}
+        nu = max(NU_MIN_LU, u * length / re)
+        out.append(Tunnel((nx, ny, nz), kind, body, re, 0.5 + 3 * nu, length, note))
+    return out

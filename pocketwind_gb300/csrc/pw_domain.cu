@@ -748,3 +748,25 @@ int pw_time_steps(pw_domain *d, uint64_t count, float *ms) {
 }
 
 }  // extern "C"
+
+namespace pwhost {
+MemberView member_view(const pw_domain *d) {
+  MemberView v;
+  v.split = d->split;
+  v.storage = d->desc.storage;
+  v.op = d->desc.op;
+  v.les = d->desc.les;
+  v.nx = d->nx; v.ny = d->ny; v.nz = d->nz;
+  v.steps = d->steps;
+  v.ramping = d->desc.ramp_steps > 0 && d->steps < d->desc.ramp_steps;
+  v.edges = d->edges;
+  v.edge_count = d->edge_count;
+  v.status = d->status_dev;
+  v.stream = d->stream;
+  return v;
+}
+pw::StepParams member_params(const pw_domain *d, uint64_t step, int write_macro) {
+  return params_for(d, step, d->u_in, write_macro);
+}
+void member_advance(pw_domain *d, uint64_t n) { d->steps += n; }
+}  // namespace pwhost

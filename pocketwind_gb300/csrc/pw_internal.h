@@ -34,6 +34,24 @@ struct DomainView {
 };
 DomainView domain_view(const pw_domain *d);
 
+// What a batch needs of a member domain (pw_batch.cu).
+struct MemberView {
+  bool split;                // fast build, one cell per thread (plain kernels + edge list)
+  int storage, op, les;
+  uint32_t nx, ny, nz;
+  uint64_t steps;
+  bool ramping;              // inlet ramp still in progress
+  const uint32_t *edges;
+  uint32_t edge_count;
+  uint32_t *status;
+  cudaStream_t stream;
+};
+MemberView member_view(const pw_domain *d);
+// The step parameters of step `step` (1-based) at the domain's full inlet speed.
+pw::StepParams member_params(const pw_domain *d, uint64_t step, int write_macro);
+// Count `n` steps run for the domain by a batch.
+void member_advance(pw_domain *d, uint64_t n);
+
 // Device-resident packed geometry (the reference's VoxelGrid).
 struct Grid {
   uint32_t nx = 0, ny = 0, nz = 0;

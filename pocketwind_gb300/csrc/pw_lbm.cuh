@@ -515,7 +515,10 @@ __device__ __forceinline__ float4 outlet_velocity_of(const typename Store<ST>::T
 }
 
 // Block reduction of the momentum exchange into this block's partial slot.
-__device__ __forceinline__ void reduce_force(bool any, double fx, double fy, double fz, double *partials) {
+// Block reduction of the momentum exchange into partial slot `slot`; t is the
+// thread's index in its block of NTHREADS.
+__device__ __forceinline__ void reduce_force_at(bool any, double fx, double fy, double fz, double *partials,
+                                                size_t slot, uint32_t t) {
   if (partials == nullptr) return;  // uniform: a kernel parameter
   if (!__syncthreads_or(any)) return;
   __shared__ double red[NTHREADS / 32][3];
@@ -525,18 +528,22 @@ __device__ __forceinline__ void reduce_force(bool any, double fx, double fy, dou
     fy += __shfl_down_sync(0xffffffffu, fy, o);
     fz += __shfl_down_sync(0xffffffffu, fz, o);
   }
-  int t = threadIdx.x + BX * threadIdx.y;
   if ((t & 31) == 0) { red[t >> 5][0] = fx; red[t >> 5][1] = fy; red[t >> 5][2] = fz; }
   __syncthreads();
   if (t == 0) {
     double a = 0, b = 0, c = 0;
 #pragma unroll
     for (int w = 0; w < NTHREADS / 32; w++) { a += red[w][0]; b += red[w][1]; c += red[w][2]; }
-    size_t blk = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * blockIdx.z);
-    partials[3 * blk + 0] = a;
-    partials[3 * blk + 1] = b;
-    partials[3 * blk + 2] = c;
+    partials[3 * slot + 0] = a;
+    partials[3 * slot + 1] = b;
+    partials[3 * slot + 2] = c;
   }
+}
+
+// Block reduction of the momentum exchange into this block's partial slot.
+__device__ __forceinline__ void reduce_force(bool any, double fx, double fy, double fz, double *partials) {
+  size_t blk = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * blockIdx.z);
+  reduce_force_at(any, fx, fy, fz, partials, blk, threadIdx.x + BX * threadIdx.y);
 }
 
 // ---------------------------------------------------------------- the step
@@ -811,12 +818,9 @@ __device__ __forceinline__ void plain_pair(const StepParams &p, uint32_t n, uint
 // touch only the cell's own slots) or of the rows off the periodic y and z
 // seams (odd steps: y and z from 1 to n-2); threads take x and x + 32 of a
 // 64-cell run of a row.
+// One thread of the plain kernel: cells x and x + 32 of row (y, z).
 template <int ST, int OP, bool LES, bool ODD>
-__global__ void __launch_bounds__(NTHREADS) aa_step_fast(StepParams p) {
-  const uint32_t x = blockIdx.x * (2 * BX) + threadIdx.x;
-  const uint32_t y = blockIdx.y * BY + threadIdx.y + (ODD ? 1u : 0u);
-  const uint32_t z = blockIdx.z + (ODD ? 1u : 0u);
-  if (y + (ODD ? 1u : 0u) >= p.ny) return;
+__device__ __forceinline__ void plain_thread(const StepParams &p, uint32_t x, uint32_t y, uint32_t z) {
   const uint32_t n = x + p.nx * (y + p.ny * z);
   uint32_t ok = 0u, eq = 0u;
 #pragma unroll
@@ -833,6 +837,15 @@ __global__ void __launch_bounds__(NTHREADS) aa_step_fast(StepParams p) {
   if (ok) plain_pair<ST, OP, LES, ODD>(p, n, x, y, z, ok, eq);
 }
 
+template <int ST, int OP, bool LES, bool ODD>
+__global__ void __launch_bounds__(NTHREADS) aa_step_fast(StepParams p) {
+  const uint32_t x = blockIdx.x * (2 * BX) + threadIdx.x;
+  const uint32_t y = blockIdx.y * BY + threadIdx.y + (ODD ? 1u : 0u);
+  const uint32_t z = blockIdx.z + (ODD ? 1u : 0u);
+  if (y + (ODD ? 1u : 0u) >= p.ny) return;
+  plain_thread<ST, OP, LES, ODD>(p, x, y, z);
+}
+
 // Odd steps on the seam rows: every row of the planes z = 0 and z = nz-1, then
 // the rows y = 0 and y = ny-1 of the planes between; one row per block row.
 // Neighbour offsets wrap around the domain.
@@ -842,10 +855,9 @@ __host__ __device__ __forceinline__ uint32_t seam_rows(uint32_t ny, uint32_t nz)
 }
 
 template <int ST, int OP, bool LES>
-__global__ void __launch_bounds__(BX) aa_step_seam(StepParams p) {
-  const uint32_t x = blockIdx.x * BX + threadIdx.x;
+__device__ __forceinline__ void seam_thread(const StepParams &p, uint32_t x, uint32_t r) {
   const uint32_t zs = p.nz > 1u ? 2u : 1u, ys = p.ny > 1u ? 2u : 1u;
-  uint32_t r = blockIdx.y, y, z;
+  uint32_t y, z;
   if (r < zs * p.ny) {
     z = r < p.ny ? 0u : p.nz - 1u;
     y = r < p.ny ? r : r - p.ny;
@@ -870,6 +882,11 @@ __global__ void __launch_bounds__(BX) aa_step_seam(StepParams p) {
   else plain_cell<ST, OP, LES, true>(p, n, x, y, z, ld, st);
 }
 
+template <int ST, int OP, bool LES>
+__global__ void __launch_bounds__(BX) aa_step_seam(StepParams p) {
+  seam_thread<ST, OP, LES>(p, blockIdx.x * BX + threadIdx.x, blockIdx.y);
+}
+
 __device__ __forceinline__ void cell_coords(const StepParams &p, uint32_t n, uint32_t &x, uint32_t &y, uint32_t &z) {
   const uint32_t row = n / p.nx;
   x = n - row * p.nx;
@@ -879,8 +896,9 @@ __device__ __forceinline__ void cell_coords(const StepParams &p, uint32_t n, uin
 
 // One listed cell per thread; block b's force partial goes to slot b.
 template <int ST, int OP, bool LES, bool ODD>
-__global__ void __launch_bounds__(NTHREADS) aa_step_edges(StepParams p, const uint32_t *list, uint32_t count) {
-  const uint32_t t = blockIdx.x * NTHREADS + threadIdx.x;
+__device__ __forceinline__ void edge_block(const StepParams &p, const uint32_t *list, uint32_t count, uint32_t blk,
+                                           uint32_t tid) {
+  const uint32_t t = blk * NTHREADS + tid;
   bool force_any = false;
   double fx = 0.0, fy = 0.0, fz = 0.0;
   if (t < count) {
@@ -889,7 +907,12 @@ __global__ void __launch_bounds__(NTHREADS) aa_step_edges(StepParams p, const ui
     cell_coords(p, n, x, y, z);
     general_cell<ST, OP, LES, ODD>(p, x, y, z, n, __ldg(&p.flags[n]), fx, fy, fz, force_any);
   }
-  reduce_force(force_any, fx, fy, fz, p.partials);
+  reduce_force_at(force_any, fx, fy, fz, p.partials, blk, tid);
+}
+
+template <int ST, int OP, bool LES, bool ODD>
+__global__ void __launch_bounds__(NTHREADS) aa_step_edges(StepParams p, const uint32_t *list, uint32_t count) {
+  edge_block<ST, OP, LES, ODD>(p, list, count, blockIdx.x, threadIdx.x);
 }
 #endif
 

@@ -1,0 +1,109 @@
+"""Batched stepping (pw_batch_*): members stepped together match the same
+domains stepped alone; the autotuner keeps a working shape; misuse is refused.
+The seeded case builder is checked on the CPU."""
+import numpy as np
+import pytest
+
+from pocketwind_gb300 import cases
+
+
+def test_splitmix64_known_answer():
+    """splitmix64 seeded 0 (Steele, Lea and Flood): first outputs."""
+    r = cases.SplitMix64(0)
+    assert r.next() == 0xE220A8397B1DCDAF
+    assert r.next() == 0x6E789E6AA1B965F4
+
+
+def test_batch_tunnels_are_seeded_and_in_range():
+    a, b = cases.batch_tunnels(64, 1), cases.batch_tunnels(64, 1)
+    assert [t.layout for t in a] == [t.layout for t in b] and [t.re for t in a] == [t.re for t in b]
+    assert {t.layout for t in a} <= set(cases.BATCH_SIZES)
+    assert all(20 <= t.re <= 300 and t.tau0 >= 0.53 for t in a)
+    assert {t.shape for t in a} == {"sphere", "ellipsoid", "box"}
+
+
+def _norm_err(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 2.0 ** -23)
+
+
+def _l2_err(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def _make(tunnel, precision, lateral="periodic"):
+    from pocketwind_gb300 import geometry, solver
+    grid = geometry.voxelize(tunnel.body, None, tunnel.layout, False)
+    return solver.GpuSolver.create(tunnel.layout, grid, solver.SolverParams(
+        tau0=tunnel.tau0, u_in=0.05, precision=precision, lateral=lateral))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["f32", "f16"])
+def test_batched_members_match_solo_runs(precision):
+    from pocketwind_gb300.batch import Batch
+    tunnels = cases.batch_tunnels(5, 3)
+    solo = [_make(t, precision) for t in tunnels]
+    together = [_make(t, precision) for t in tunnels]
+    batch = Batch(together)
+    for s in solo:
+        s.step(57, True)
+    batch.step(57, True)  # a captured 50-step graph, then 7 single launches
+    for a, b in zip(together, solo):
+        assert a.step_count == b.step_count == 57
+        if precision == "f32":
+            assert _norm_err(a.populations(), b.populations()) < 1e-5
+            assert _norm_err(a.macros()[:, 1:], b.macros()[:, 1:]) < 1e-5
+        else:
+            # the batch kernel may fuse multiply-adds differently, and a last-bit
+            # difference changes a code's dither: 16-bit states drift apart by a
+            # few storage units per cell, so they are compared in relative L2
+            assert _l2_err(a.populations(), b.populations()) < 1e-3
+            assert _l2_err(a.macros()[:, 1:], b.macros()[:, 1:]) < 1e-3
+        a.encode_force()
+        b.encode_force()
+        fa, fb = a.read_force(), b.read_force()
+        assert fa.step == fb.step == 57
+        assert abs(fa.fx - fb.fx) <= (1e-4 if precision == "f32" else 2e-3) * max(abs(fb.fx), 1e-6)
+    batch.destroy()
+
+
+@pytest.mark.gpu
+def test_tuning_keeps_a_working_shape_and_reset_restarts():
+    from pocketwind_gb300.batch import Batch
+    tunnels = cases.batch_tunnels(4, 7)
+    members = [_make(t, "f16") for t in tunnels]
+    batch = Batch(members)
+    t = batch.tune(4)
+    assert t.candidates == 15 and t.rows_per_item in (4, 8, 16) and t.blocks > 0 and t.ms_per_step > 0
+    batch.reset()
+    solo = [_make(x, "f16") for x in tunnels]
+    batch.step(20, True)
+    for s in solo:
+        s.step(20, True)
+    for a, b in zip(members, solo):
+        assert _l2_err(a.macros()[:, 1:], b.macros()[:, 1:]) < 1e-3
+    assert batch.time_steps(10) > 0
+    batch.destroy()
+
+
+@pytest.mark.gpu
+def test_batch_refuses_mixed_or_misused_members():
+    from pocketwind_gb300 import geometry, solver
+    from pocketwind_gb300.batch import Batch
+    t = cases.batch_tunnels(2, 5)
+    a, b = _make(t[0], "f16"), _make(t[1], "f32")
+    with pytest.raises(solver.RangeError):
+        Batch([a, b])
+    c = _make(t[1], "f16")
+    grid = geometry.voxelize(t[0].body, None, t[0].layout, False)
+    strict = solver.GpuSolver.create(t[0].layout, grid, solver.SolverParams(tau0=t[0].tau0, u_in=0.05,
+                                                                             precision="f16", strict=True))
+    with pytest.raises(solver.RangeError):
+        Batch([a, strict])
+    batch = Batch([a, c])
+    a.step(1)
+    with pytest.raises(solver.RangeError):
+        batch.step(1)
+    batch.destroy()
