@@ -228,6 +228,39 @@ PW_API int pw_batch_tune(pw_batch *batch, uint32_t trial_steps, pw_batch_tuning 
 /* pw_reset of every member; the batch starts again at step 0. */
 PW_API int pw_batch_reset(pw_batch *batch);
 
+/* ---- the learned subgrid closure (no counterpart in the reference) ----
+   A 9 -> 32 -> 32 -> 1 network scales the Smagorinsky eddy viscosity of plain
+   LES cells by max(0, 1 + c); c = 0 (the untrained network) is Smagorinsky.
+   Parameters: W1[32][9] b1[32] W2[32][32] b2[32] W3[32] b3 (1409 floats),
+   bfloat16 in the forward pass with binary32 accumulation. */
+typedef struct pw_closure pw_closure;
+#define PW_CLOSURE_PARAMS 1409
+#define PW_CLOSURE_INPUTS 9
+PW_API int pw_closure_create(uint64_t seed, pw_closure **out);
+PW_API void pw_closure_destroy(pw_closure *c);
+PW_API int pw_closure_get_params(pw_closure *c, float *out);
+PW_API int pw_closure_set_params(pw_closure *c, const float *in);
+/* network outputs for count input rows (9 floats each), the fused kernel's path */
+PW_API int pw_closure_eval(pw_closure *c, const float *x, uint32_t count, float *out);
+/* one forward and backward pass over count samples: parameter gradients of the
+   mean squared error, and that error */
+PW_API int pw_closure_gradients(pw_closure *c, const float *x, const float *y, uint32_t count, float *grad,
+                                float *loss);
+/* training data: samples from a fine domain's latest macros, box-filtered 2x
+   onto the coarse grid whose molecular viscosity is nu0_coarse */
+PW_API int pw_closure_dataset_add(pw_closure *c, pw_domain *fine, double nu0_coarse, uint64_t *added);
+PW_API int pw_closure_dataset_clear(pw_closure *c);
+PW_API int pw_closure_dataset_reserve(pw_closure *c, uint64_t capacity);
+PW_API int pw_closure_dataset_write(pw_closure *c, const float *x, const float *y, uint64_t count);
+PW_API int pw_closure_dataset_size(const pw_closure *c, uint64_t *n);
+PW_API int pw_closure_dataset_read(pw_closure *c, uint64_t first, uint64_t count, float *x, float *y);
+/* Adam (lr, betas 0.9 / 0.999) over `steps` minibatches drawn by a seeded hash */
+PW_API int pw_closure_train(pw_closure *c, uint32_t steps, uint32_t batch, float lr, uint64_t seed,
+                            float *loss_first, float *loss_last);
+/* Attach (c) or detach (NULL) a closure to an LES domain of the fast build; the
+   domain restarts from its initial state.  The closure must outlive the attachment. */
+PW_API int pw_closure_attach(pw_domain *dom, const pw_closure *c);
+
 PW_API int pw_time_steps(pw_domain *dom, uint64_t count, float *ms);
 /* Queue `count` steps (no graphs) with CUDA events around each launch class and
    sum their device times: kernel_ms[0] the plain-cell kernel, [1] its seam-row

@@ -85,6 +85,21 @@ SIGNATURES = {
     "pw_batch_time_steps": (_int, [_vp, _u64, C.POINTER(C.c_float)]),
     "pw_batch_tune": (_int, [_vp, C.c_uint32, C.c_void_p]),
     "pw_batch_reset": (_int, [_vp]),
+    "pw_closure_create": (_int, [_u64, C.POINTER(_vp)]),
+    "pw_closure_destroy": (None, [_vp]),
+    "pw_closure_get_params": (_int, [_vp, _vp]),
+    "pw_closure_set_params": (_int, [_vp, _vp]),
+    "pw_closure_eval": (_int, [_vp, _vp, C.c_uint32, _vp]),
+    "pw_closure_gradients": (_int, [_vp, _vp, _vp, C.c_uint32, _vp, C.POINTER(C.c_float)]),
+    "pw_closure_dataset_add": (_int, [_vp, _vp, C.c_double, C.POINTER(_u64)]),
+    "pw_closure_dataset_clear": (_int, [_vp]),
+    "pw_closure_dataset_reserve": (_int, [_vp, _u64]),
+    "pw_closure_dataset_write": (_int, [_vp, _vp, _vp, _u64]),
+    "pw_closure_dataset_size": (_int, [_vp, C.POINTER(_u64)]),
+    "pw_closure_dataset_read": (_int, [_vp, _u64, _u64, _vp, _vp]),
+    "pw_closure_train": (_int, [_vp, C.c_uint32, C.c_uint32, C.c_float, _u64, C.POINTER(C.c_float),
+                                C.POINTER(C.c_float)]),
+    "pw_closure_attach": (_int, [_vp, _vp]),
     "pw_particles_create": (_int, [_vp, _vp, _u32, _u32, _vp, _vp, _PP]),
     "pw_particles_update": (_int, [_vp, _f32]),
     "pw_particles_read": (_int, [_vp, _vp]),

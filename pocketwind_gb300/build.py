@@ -31,8 +31,9 @@ UNITS = {
     "pw_domain.cu": [],
     "pw_noalloc.cu": [],
     "pw_batch.cu": [],
+    "pw_closure.cu": [],
 }
-HEADERS = ["pw_common.cuh", "pw_lbm.cuh", "pw_lbm_tile.cuh", "pw_launch.h", "pw_internal.h"]
+HEADERS = ["pw_common.cuh", "pw_lbm.cuh", "pw_lbm_tile.cuh", "pw_launch.h", "pw_internal.h", "pw_closure.cuh"]
 
 
 def nvcc() -> str:

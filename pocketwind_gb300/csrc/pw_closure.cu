@@ -1,0 +1,880 @@
+// The learned subgrid closure (pw_closure_*): training data from the solver's
+// own fine-grid fields, hand-written training (forward, backward, Adam), and
+// inference fused into a step kernel on the tensor cores.  No counterpart in
+// the reference.
+//
+// Data: a fine run's macros are box-filtered 2x2x2 onto the coarse grid; the
+// target is the eddy viscosity that best reproduces the subgrid stress of the
+// filtered fields, nu* = max(0, -tau_sgs : S / (2 S : S)), with
+// tau_sgs = mean((u - ubar)(u - ubar)) and S the finite-difference strain of the
+// filtered velocity, expressed as c* = nu* / nu_smag - 1 (clipped to [-1, 3]),
+// nu_smag = (0.1)^2 |S| the Smagorinsky viscosity of the same strain.  Cells
+// within two coarse cells of a wall or of the x faces are left out (the wall
+// model owns the wall cells).
+//
+// Inference (closure_step): one cell per thread; a first pass takes each plain
+// LES cell's Smagorinsky state from its populations, its strain
+// S = -3 Pi_neq / (2 rho tau_s) and the nine inputs; each warp then runs the
+// network for its 32 cells as a chain of mma.sync m16n8k16 bf16 products
+// (28 per warp, layers chained in registers); the second pass is the ordinary
+// cell update with tau = tau0 + (tau_s - tau0) max(0, 1 + c).
+#define PW_NS pwclosure
+#define PW_STRICT 0
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "pw_internal.h"
+#include "pw_lbm.cuh"
+#include "pw_closure.cuh"
+#include "pw_launch.h"
+
+using namespace pwhost;
+using pw::StepParams;
+using namespace pwcl;
+
+namespace {
+
+constexpr int kFragWords = 48;  // per lane: W1 8, W2 16, W3 4, b1 8, b2 8, b3 1 (+3)
+constexpr int kTrainThreads = 128;
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t *>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], const uint32_t b[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// Per-lane operand fragments of the three layers (B = W^T, "col" layout: lane
+// (g, t) holds B[2t, 2t+1][g] and B[2t+8, 2t+9][g] of each 16 x 8 tile) and
+// the biases in the accumulator layout (columns 2t, 2t+1 of each 8-wide tile).
+__global__ void build_fragments(const float *w, uint32_t *frag) {
+  const uint32_t lane = threadIdx.x, g = lane >> 2, t = lane & 3;
+  uint32_t *o = frag + lane * kFragWords;
+  auto w1 = [&](uint32_t n, uint32_t k) { return k < (uint32_t)kIn ? w[kW1 + n * kIn + k] : 0.0f; };
+  auto w2 = [&](uint32_t n, uint32_t k) { return w[kW2 + n * kHidden + k]; };
+  auto w3 = [&](uint32_t k) { return g == 0 ? w[kW3 + k] : 0.0f; };
+  for (uint32_t j = 0; j < 4; j++) {
+    const uint32_t n = 8 * j + g;
+    o[2 * j] = pack_bf16(w1(n, 2 * t), w1(n, 2 * t + 1));
+    o[2 * j + 1] = pack_bf16(w1(n, 2 * t + 8), w1(n, 2 * t + 9));
+    for (uint32_t kt = 0; kt < 2; kt++) {
+      const uint32_t kb = 16 * kt;
+      o[8 + (2 * j + kt) * 2] = pack_bf16(w2(n, kb + 2 * t), w2(n, kb + 2 * t + 1));
+      o[8 + (2 * j + kt) * 2 + 1] = pack_bf16(w2(n, kb + 2 * t + 8), w2(n, kb + 2 * t + 9));
+    }
+    o[28 + 2 * j] = __float_as_uint(w[kB1 + 8 * j + 2 * t]);
+    o[29 + 2 * j] = __float_as_uint(w[kB1 + 8 * j + 2 * t + 1]);
+    o[36 + 2 * j] = __float_as_uint(w[kB2 + 8 * j + 2 * t]);
+    o[37 + 2 * j] = __float_as_uint(w[kB2 + 8 * j + 2 * t + 1]);
+  }
+  for (uint32_t kt = 0; kt < 2; kt++) {
+    o[24 + 2 * kt] = pack_bf16(w3(16 * kt + 2 * t), w3(16 * kt + 2 * t + 1));
+    o[25 + 2 * kt] = pack_bf16(w3(16 * kt + 2 * t + 8), w3(16 * kt + 2 * t + 9));
+  }
+  o[44] = __float_as_uint(w[kB3]);
+  o[45] = o[46] = o[47] = 0u;
+}
+
+// The network on the 32 cells of a warp (every lane must call; `x` is this
+// lane's input row, `stage` 256 words of shared memory owned by the warp).
+__device__ float warp_mlp(const uint32_t *frag, const float x[kIn], uint32_t *stage) {
+  const uint32_t lane = threadIdx.x & 31u, g = lane >> 2, t = lane & 3;
+  const uint32_t *fr = frag + lane * kFragWords;
+  uint32_t w1[8], w2[16], w3[4];
+  float b1[8], b2[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) w1[k] = __ldg(&fr[k]);
+#pragma unroll
+  for (int k = 0; k < 16; k++) w2[k] = __ldg(&fr[8 + k]);
+#pragma unroll
+  for (int k = 0; k < 4; k++) w3[k] = __ldg(&fr[24 + k]);
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    b1[k] = __uint_as_float(__ldg(&fr[28 + k]));
+    b2[k] = __uint_as_float(__ldg(&fr[36 + k]));
+  }
+  const float b3 = __uint_as_float(__ldg(&fr[44]));
+  // stage the inputs: row `lane`, word k = inputs 2k, 2k+1 (inputs 9..15 are zero)
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const float lo = 2 * k < kIn ? x[2 * k] : 0.0f, hi = 2 * k + 1 < kIn ? x[2 * k + 1] : 0.0f;
+    stage[lane * 8 + k] = pack_bf16(lo, hi);
+  }
+  __syncwarp();
+  float out_lo[2], out_hi[2];
+#pragma unroll
+  for (int m = 0; m < 2; m++) {
+    const uint32_t r0 = 16 * m + g, r1 = r0 + 8;
+    const uint32_t a[4] = {stage[r0 * 8 + t], stage[r1 * 8 + t], stage[r0 * 8 + 4 + t], stage[r1 * 8 + 4 + t]};
+    float h[4][4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      h[j][0] = b1[2 * j]; h[j][1] = b1[2 * j + 1]; h[j][2] = b1[2 * j]; h[j][3] = b1[2 * j + 1];
+      mma_bf16(h[j], a, &w1[2 * j]);
+    }
+    uint32_t a2[2][4];
+#pragma unroll
+    for (int kt = 0; kt < 2; kt++) {
+      a2[kt][0] = pack_bf16(tanh_fast(h[2 * kt][0]), tanh_fast(h[2 * kt][1]));
+      a2[kt][1] = pack_bf16(tanh_fast(h[2 * kt][2]), tanh_fast(h[2 * kt][3]));
+      a2[kt][2] = pack_bf16(tanh_fast(h[2 * kt + 1][0]), tanh_fast(h[2 * kt + 1][1]));
+      a2[kt][3] = pack_bf16(tanh_fast(h[2 * kt + 1][2]), tanh_fast(h[2 * kt + 1][3]));
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      h[j][0] = b2[2 * j]; h[j][1] = b2[2 * j + 1]; h[j][2] = b2[2 * j]; h[j][3] = b2[2 * j + 1];
+      mma_bf16(h[j], a2[0], &w2[(2 * j) * 2]);
+      mma_bf16(h[j], a2[1], &w2[(2 * j + 1) * 2]);
+    }
+#pragma unroll
+    for (int kt = 0; kt < 2; kt++) {
+      a2[kt][0] = pack_bf16(tanh_fast(h[2 * kt][0]), tanh_fast(h[2 * kt][1]));
+      a2[kt][1] = pack_bf16(tanh_fast(h[2 * kt][2]), tanh_fast(h[2 * kt][3]));
+      a2[kt][2] = pack_bf16(tanh_fast(h[2 * kt + 1][0]), tanh_fast(h[2 * kt + 1][1]));
+      a2[kt][3] = pack_bf16(tanh_fast(h[2 * kt + 1][2]), tanh_fast(h[2 * kt + 1][3]));
+    }
+    float o[4] = {t == 0 ? b3 : 0.0f, 0.0f, t == 0 ? b3 : 0.0f, 0.0f};
+    mma_bf16(o, a2[0], &w3[0]);
+    mma_bf16(o, a2[1], &w3[2]);
+    out_lo[m] = o[0];
+    out_hi[m] = o[2];
+  }
+  __syncwarp();
+  float *res = reinterpret_cast<float *>(stage);
+  if (t == 0) {
+#pragma unroll
+    for (int m = 0; m < 2; m++) {
+      res[16 * m + g] = out_lo[m];
+      res[16 * m + g + 8] = out_hi[m];
+    }
+  }
+  __syncwarp();
+  const float c = res[lane];
+  __syncwarp();
+  return c;
+}
+
+// Records the Smagorinsky state of a cell (first pass).
+struct CaptureHook {
+  float *s;  // tau_s, rho, ux, uy, uz, pxx, pyy, pzz, pxy, pxz, pyz
+  __device__ __forceinline__ float operator()(const StepParams &, float tau_s, float rho, float vx, float vy, float vz,
+                                              float pxx, float pyy, float pzz, float pxy, float pxz,
+                                              float pyz) const {
+    s[0] = tau_s; s[1] = rho; s[2] = vx; s[3] = vy; s[4] = vz;
+    s[5] = pxx; s[6] = pyy; s[7] = pzz; s[8] = pxy; s[9] = pxz; s[10] = pyz;
+    return tau_s;
+  }
+};
+
+// Scales the Smagorinsky eddy viscosity by max(0, 1 + c) (second pass).
+struct ClosureHook {
+  float c;
+  __device__ __forceinline__ float operator()(const StepParams &p, float tau_s, float, float, float, float, float,
+                                              float, float, float, float, float) const {
+    return p.tau0 + (tau_s - p.tau0) * fmaxf(0.0f, 1.0f + c);
+  }
+};
+
+// Inputs of a cell from its Smagorinsky state (strain from the stress).
+__device__ __forceinline__ void cell_inputs(const StepParams &p, const float *st, float wall, float x[kIn]) {
+  const float tau_s = st[0], rho = st[1];
+  const float k = -1.5f / (rho * tau_s);  // S = -Pi / (2 rho c_s^2 tau), c_s^2 = 1/3
+  const float s[6] = {k * st[5], k * st[6], k * st[7], k * st[8], k * st[9], k * st[10]};
+  const float nu_s = (tau_s - p.tau0) * (1.0f / 3.0f);
+  features(s, rho, st[2], st[3], st[4], wall, p.nu, nu_s, p.u_in, x);
+}
+
+template <int ST, int OP, bool ODD>
+__global__ void __launch_bounds__(128) closure_step(StepParams p, const uint32_t *frag, const uint8_t *wall_dist) {
+  using S = pw::Store<ST>;
+  using T = typename S::T;
+  __shared__ uint32_t stage[4][256];
+  const uint32_t x = blockIdx.x * 32 + threadIdx.x;
+  const uint32_t y = blockIdx.y * 4 + threadIdx.y;
+  const uint32_t z = blockIdx.z;
+  const bool in = x < p.nx && y < p.ny;
+  const uint32_t n = in ? x + p.nx * (y + p.ny * z) : 0u;
+  const uint32_t flag = in ? __ldg(&p.flags[n]) : (uint32_t)pw::SOLID;
+  float xin[kIn];
+#pragma unroll
+  for (int k = 0; k < kIn; k++) xin[k] = 0.0f;
+  const bool plain = in && flag == pw::FLUID;  // fluid without wall links
+  if (plain) {
+    const T *f = reinterpret_cast<const T *>(p.f);
+    const pwclosure::Nbr b = pwclosure::make_nbr(p, x, y, z);
+    float g[19];
+#pragma unroll
+    for (int i = 0; i < 19; i++) g[i] = S::decode(f[ODD ? b.pull(i, p.stride) : (uint32_t)i * p.stride + n]);
+    float st[11], rho, vx, vy, vz;
+    pwclosure::update_fast<OP, true, CaptureHook>(p, g, rho, vx, vy, vz, 1.0f, 1.0f, CaptureHook{st});
+    cell_inputs(p, st, (float)wall_dist[n], xin);
+  }
+  const float c = warp_mlp(frag, xin, stage[threadIdx.y]);
+  bool any = false;
+  double fx = 0.0, fy = 0.0, fz = 0.0;
+  if (in) pwclosure::general_cell<ST, OP, true, ODD, ClosureHook>(p, x, y, z, n, flag, fx, fy, fz, any, ClosureHook{c});
+  pwclosure::reduce_force(any, fx, fy, fz, p.partials);
+}
+
+// Network outputs for given inputs through the same warp path (tests).
+__global__ void eval_kernel(const uint32_t *frag, const float *xin, uint32_t count, float *out) {
+  __shared__ uint32_t stage[4][256];
+  const uint32_t i = blockIdx.x * 128 + threadIdx.x;
+  float x[kIn];
+#pragma unroll
+  for (int k = 0; k < kIn; k++) x[k] = i < count ? xin[(size_t)i * kIn + k] : 0.0f;
+  const float c = warp_mlp(frag, x, stage[threadIdx.x >> 5]);
+  if (i < count) out[i] = c;
+}
+
+// ---------------------------------------------------------------- wall distance
+// Cells to the nearest wall cell (6-neighbour steps, capped at kWallCap): x
+// bounded, y and z periodic as the lattice.
+__global__ void dist_init(const uint32_t *flags, size_t cells, uint8_t *d) {
+  const size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n < cells) d[n] = pw::is_wall_kind(flags[n] & 7u) ? 0 : 255;
+}
+__global__ void dist_from_solid(const uint8_t *solid, size_t cells, uint8_t *d) {
+  const size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n < cells) d[n] = solid[n] ? 0 : 255;
+}
+__global__ void dist_step(const uint8_t *in, uint8_t *out, uint32_t nx, uint32_t ny, uint32_t nz) {
+  const size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= (size_t)nx * ny * nz) return;
+  const uint32_t x = (uint32_t)(n % nx), y = (uint32_t)((n / nx) % ny), z = (uint32_t)(n / ((size_t)nx * ny));
+  const size_t plane = (size_t)nx * ny;
+  uint32_t v = in[n];
+  if (x > 0) v = min(v, in[n - 1] + 1u);
+  if (x + 1 < nx) v = min(v, in[n + 1] + 1u);
+  v = min(v, in[n - (size_t)y * nx + (size_t)((y + ny - 1) % ny) * nx] + 1u);
+  v = min(v, in[n - (size_t)y * nx + (size_t)((y + 1) % ny) * nx] + 1u);
+  v = min(v, in[n - (size_t)z * plane + (size_t)((z + nz - 1) % nz) * plane] + 1u);
+  v = min(v, in[n - (size_t)z * plane + (size_t)((z + 1) % nz) * plane] + 1u);
+  out[n] = (uint8_t)min(v, 255u);
+}
+
+int wall_distance(uint8_t *d, uint8_t *tmp, uint32_t nx, uint32_t ny, uint32_t nz, cudaStream_t s) {
+  const size_t cells = (size_t)nx * ny * nz;
+  const unsigned blocks = (unsigned)((cells + 255) / 256);
+  for (int k = 0; k < (int)kWallCap; k += 2) {
+    dist_step<<<blocks, 256, 0, s>>>(d, tmp, nx, ny, nz);
+    dist_step<<<blocks, 256, 0, s>>>(tmp, d, nx, ny, nz);
+  }
+  PW_TRY(cudaGetLastError());
+  return PW_OK;
+}
+
+// ---------------------------------------------------------------- training data
+// coarse[q][N]: rho, ux, uy, uz and the subgrid stress mean((u - ubar)(u - ubar)):
+// xx, yy, zz, xy, xz, yz (taken from the deviations, free of the cancellation
+// of mean(u u) - ubar ubar in binary32).
+__global__ void coarsen_kernel(const float4 *macros, const uint32_t *flags, uint32_t nx, uint32_t ny, uint32_t nz,
+                               float *coarse, uint8_t *solid) {
+  const uint32_t cx = nx / 2, cy = ny / 2, cz = nz / 2;
+  const size_t nc = (size_t)cx * cy * cz;
+  const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const uint32_t X = (uint32_t)(c % cx), Y = (uint32_t)((c / cx) % cy), Z = (uint32_t)(c / ((size_t)cx * cy));
+  float4 m[8];
+  float mean[4] = {0, 0, 0, 0};
+  uint32_t walls = 0;
+  for (uint32_t k = 0; k < 8; k++) {
+    const size_t n = (2 * X + (k & 1)) + (size_t)nx * ((2 * Y + ((k >> 1) & 1)) + (size_t)ny * (2 * Z + (k >> 2)));
+    m[k] = macros[n];
+    walls += pw::is_wall_kind(flags[n] & 7u) ? 1u : 0u;
+    mean[0] += m[k].x; mean[1] += m[k].y; mean[2] += m[k].z; mean[3] += m[k].w;
+  }
+  for (int q = 0; q < 4; q++) mean[q] *= 0.125f;
+  float t[6] = {0, 0, 0, 0, 0, 0};
+  for (uint32_t k = 0; k < 8; k++) {
+    const float dx = m[k].y - mean[1], dy = m[k].z - mean[2], dz = m[k].w - mean[3];
+    t[0] += dx * dx; t[1] += dy * dy; t[2] += dz * dz; t[3] += dx * dy; t[4] += dx * dz; t[5] += dy * dz;
+  }
+  for (int q = 0; q < 4; q++) coarse[(size_t)q * nc + c] = mean[q];
+  for (int q = 0; q < 6; q++) coarse[(size_t)(4 + q) * nc + c] = 0.125f * t[q];
+  solid[c] = walls ? 1 : 0;
+}
+
+// Target and inputs of coarse cell c, or false when it is left out.
+__device__ __forceinline__ bool coarse_sample(const float *co, const uint8_t *dist, uint32_t cx, uint32_t cy,
+                                              uint32_t cz, size_t c, float nu0, float u_in, float x[kIn], float *y) {
+  const size_t nc = (size_t)cx * cy * cz;
+  const uint32_t X = (uint32_t)(c % cx), Y = (uint32_t)((c / cx) % cy), Z = (uint32_t)(c / ((size_t)cx * cy));
+  if (X < 2 || X + 3 > cx || dist[c] < 2) return false;
+  const size_t plane = (size_t)cx * cy;
+  const size_t xm = c - 1, xp = c + 1;
+  const size_t ym = c - (size_t)Y * cx + (size_t)((Y + cy - 1) % cy) * cx, yp = c - (size_t)Y * cx + (size_t)((Y + 1) % cy) * cx;
+  const size_t zm = c - (size_t)Z * plane + (size_t)((Z + cz - 1) % cz) * plane;
+  const size_t zp = c - (size_t)Z * plane + (size_t)((Z + 1) % cz) * plane;
+  auto u = [&](int comp, size_t at) { return co[(size_t)(1 + comp) * nc + at]; };
+  float grad[3][3];  // grad[a][b] = d u_b / d x_a
+  for (int b = 0; b < 3; b++) {
+    grad[0][b] = 0.5f * (u(b, xp) - u(b, xm));
+    grad[1][b] = 0.5f * (u(b, yp) - u(b, ym));
+    grad[2][b] = 0.5f * (u(b, zp) - u(b, zm));
+  }
+  const float s[6] = {grad[0][0], grad[1][1], grad[2][2], 0.5f * (grad[0][1] + grad[1][0]),
+                      0.5f * (grad[0][2] + grad[2][0]), 0.5f * (grad[1][2] + grad[2][1])};
+  const float ux = u(0, c), uy = u(1, c), uz = u(2, c);
+  const float tsgs[6] = {co[4 * nc + c], co[5 * nc + c], co[6 * nc + c], co[7 * nc + c], co[8 * nc + c],
+                         co[9 * nc + c]};
+  const float ss = s[0] * s[0] + s[1] * s[1] + s[2] * s[2] + 2.0f * (s[3] * s[3] + s[4] * s[4] + s[5] * s[5]);
+  const float ts = tsgs[0] * s[0] + tsgs[1] * s[1] + tsgs[2] * s[2] + 2.0f * (tsgs[3] * s[3] + tsgs[4] * s[4] + tsgs[5] * s[5]);
+  const float nu_s = 0.01f * sqrtf(2.0f * ss);
+  if (!(nu_s > 1e-9f)) return false;
+  const float nu_t = fmaxf(0.0f, -ts / (2.0f * ss));
+  *y = fminf(3.0f, fmaxf(-1.0f, nu_t / nu_s - 1.0f));
+  features(s, co[c], ux, uy, uz, (float)dist[c], nu0, nu_s, u_in, x);
+  return true;
+}
+
+constexpr int kScanBlock = 1024;
+
+__global__ void sample_count(const float *co, const uint8_t *dist, uint32_t cx, uint32_t cy, uint32_t cz, float nu0,
+                             float u_in, uint32_t *block_counts) {
+  __shared__ uint32_t warp_counts[kScanBlock / 32];
+  const size_t c = (size_t)blockIdx.x * kScanBlock + threadIdx.x;
+  float x[kIn], y;
+  const bool ok = c < (size_t)cx * cy * cz && coarse_sample(co, dist, cx, cy, cz, c, nu0, u_in, x, &y);
+  const uint32_t ballot = __ballot_sync(0xffffffffu, ok);
+  if ((threadIdx.x & 31) == 0) warp_counts[threadIdx.x >> 5] = __popc(ballot);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int w = 0; w < kScanBlock / 32; w++) t += warp_counts[w];
+    block_counts[blockIdx.x] = t;
+  }
+}
+
+__global__ void scan_counts(uint32_t *counts, uint32_t nblk, uint32_t *total) {
+  __shared__ uint32_t sh[kScanBlock];
+  uint32_t carry = 0;
+  for (uint32_t base = 0; base < nblk; base += kScanBlock) {
+    const uint32_t i = base + threadIdx.x;
+    const uint32_t v = i < nblk ? counts[i] : 0u;
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < kScanBlock; o <<= 1) {
+      const uint32_t add = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0u;
+      __syncthreads();
+      sh[threadIdx.x] += add;
+      __syncthreads();
+    }
+    if (i < nblk) counts[i] = carry + sh[threadIdx.x] - v;
+    carry += sh[kScanBlock - 1];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void sample_write(const float *co, const uint8_t *dist, uint32_t cx, uint32_t cy, uint32_t cz, float nu0,
+                             float u_in, const uint32_t *offsets, uint64_t base, uint64_t cap, float *X, float *Y) {
+  __shared__ uint32_t warp_base[kScanBlock / 32];
+  const size_t c = (size_t)blockIdx.x * kScanBlock + threadIdx.x;
+  float x[kIn], y = 0.0f;
+  const bool ok = c < (size_t)cx * cy * cz && coarse_sample(co, dist, cx, cy, cz, c, nu0, u_in, x, &y);
+  const uint32_t ballot = __ballot_sync(0xffffffffu, ok);
+  const uint32_t lane = threadIdx.x & 31;
+  if (lane == 0) warp_base[threadIdx.x >> 5] = __popc(ballot);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = offsets[blockIdx.x];
+    for (int w = 0; w < kScanBlock / 32; w++) { const uint32_t k = warp_base[w]; warp_base[w] = t; t += k; }
+  }
+  __syncthreads();
+  if (!ok) return;
+  const uint64_t at = base + warp_base[threadIdx.x >> 5] + __popc(ballot & ((1u << lane) - 1u));
+  if (at >= cap) return;
+  for (int k = 0; k < kIn; k++) X[at * kIn + k] = x[k];
+  Y[at] = y;
+}
+
+// ---------------------------------------------------------------- training
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// One block of kTrainThreads samples: forward with the network's rounding,
+// squared error against the target, backward (the bf16 roundings pass
+// gradients through unchanged; tanh' = 1 - h^2 of the rounded activation),
+// and the block's parameter-gradient sums and loss sum in partial[block].
+// sample index: explicit list `idx` when given, else mix64(seed + step * 2^32 + i) mod n.
+__global__ void __launch_bounds__(kTrainThreads) train_block(const float *w, const float *X, const float *Y, uint64_t n,
+                                                             uint32_t batch, uint64_t seed, const uint32_t *step,
+                                                             const uint32_t *idx, float *partial) {
+  extern __shared__ float sm[];
+  float *wr = sm;                                     // kParams rounded weights (biases kept)
+  float *xs = wr + kParams + 3;                       // [kTrainThreads][kIn]
+  float *h1s = xs + kTrainThreads * kIn;              // [kTrainThreads][32]
+  float *d1s = h1s + kTrainThreads * kHidden;
+  float *h2s = d1s + kTrainThreads * kHidden;
+  float *d2s = h2s + kTrainThreads * kHidden;
+  float *d3s = d2s + kTrainThreads * kHidden;         // [kTrainThreads]
+  float *ls = d3s + kTrainThreads;                    // [kTrainThreads]
+  const uint32_t tid = threadIdx.x;
+  for (int k = tid; k < kParams; k += kTrainThreads) {
+    const bool bias = (k >= kB1 && k < kW2) || (k >= kB2 && k < kW3) || k == kB3;
+    wr[k] = bias ? w[k] : bf16_round(w[k]);
+  }
+  __syncthreads();
+  const uint32_t i = blockIdx.x * kTrainThreads + tid;
+  const bool live = i < batch;
+  uint64_t s = 0;
+  if (live) s = idx ? idx[i] : mix64(seed + ((uint64_t)*step << 32) + i) % n;
+  float x[kIn], h1[kHidden];
+#pragma unroll
+  for (int k = 0; k < kIn; k++) x[k] = live ? bf16_round(X[s * kIn + k]) : 0.0f;
+  for (int j = 0; j < kHidden; j++) {
+    float a = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kIn; k++) a = fmaf(wr[kW1 + j * kIn + k], x[k], a);
+    h1[j] = bf16_round(tanh_fast(a + wr[kB1 + j]));
+  }
+  float out = 0.0f;
+  for (int j = 0; j < kHidden; j++) {
+    float a = 0.0f;
+    for (int k = 0; k < kHidden; k++) a = fmaf(wr[kW2 + j * kHidden + k], h1[k], a);
+    const float h2 = bf16_round(tanh_fast(a + wr[kB2 + j]));
+    h2s[tid * kHidden + j] = h2;
+    out = fmaf(wr[kW3 + j], h2, out);
+  }
+  out += wr[kB3];
+  const float err = live ? out - Y[s] : 0.0f;
+  const float d3 = live ? 2.0f * err / (float)batch : 0.0f;
+  ls[tid] = err * err;
+  d3s[tid] = d3;
+  for (int j = 0; j < kHidden; j++) {
+    const float h2 = h2s[tid * kHidden + j];
+    d2s[tid * kHidden + j] = d3 * wr[kW3 + j] * (1.0f - h2 * h2);
+  }
+  for (int k = 0; k < kHidden; k++) {
+    float a = 0.0f;
+    for (int j = 0; j < kHidden; j++) a = fmaf(d2s[tid * kHidden + j], wr[kW2 + j * kHidden + k], a);
+    d1s[tid * kHidden + k] = a * (1.0f - h1[k] * h1[k]);
+    h1s[tid * kHidden + k] = h1[k];
+  }
+#pragma unroll
+  for (int k = 0; k < kIn; k++) xs[tid * kIn + k] = x[k];
+  __syncthreads();
+  float *out_p = partial + (size_t)blockIdx.x * (kParams + 1);
+  for (int q = tid; q < kParams + 1; q += kTrainThreads) {
+    float acc = 0.0f;
+    if (q < kB1) {
+      const int j = q / kIn, k = q % kIn;
+      for (int r = 0; r < kTrainThreads; r++) acc = fmaf(d1s[r * kHidden + j], xs[r * kIn + k], acc);
+    } else if (q < kW2) {
+      for (int r = 0; r < kTrainThreads; r++) acc += d1s[r * kHidden + (q - kB1)];
+    } else if (q < kB2) {
+      const int j = (q - kW2) / kHidden, k = (q - kW2) % kHidden;
+      for (int r = 0; r < kTrainThreads; r++) acc = fmaf(d2s[r * kHidden + j], h1s[r * kHidden + k], acc);
+    } else if (q < kW3) {
+      for (int r = 0; r < kTrainThreads; r++) acc += d2s[r * kHidden + (q - kB2)];
+    } else if (q < kB3) {
+      for (int r = 0; r < kTrainThreads; r++) acc = fmaf(d3s[r], h2s[r * kHidden + (q - kW3)], acc);
+    } else if (q == kB3) {
+      for (int r = 0; r < kTrainThreads; r++) acc += d3s[r];
+    } else {
+      for (int r = 0; r < kTrainThreads; r++) acc += ls[r];
+    }
+    out_p[q] = acc;
+  }
+}
+
+// Fixed-order sums of the block partials: grad[q], q < kParams; grad[kParams] = loss sum.
+__global__ void train_reduce(const float *partial, uint32_t blocks, float *grad) {
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q > (uint32_t)kParams) return;
+  float acc = 0.0f;
+  for (uint32_t b = 0; b < blocks; b++) acc += partial[(size_t)b * (kParams + 1) + q];
+  grad[q] = acc;
+}
+
+// Adam (beta1 0.9, beta2 0.999, eps 1e-8) on the binary32 master weights; one
+// block, which then advances the step counter and records the batch loss.
+__global__ void train_adam(float *w, float *m, float *v, const float *grad, uint32_t *step, float lr, uint32_t batch,
+                           float *loss) {
+  const uint32_t t = *step + 1;
+  const float c1 = 1.0f - powf(0.9f, (float)t), c2 = 1.0f - powf(0.999f, (float)t);
+  for (int q = threadIdx.x; q < kParams; q += blockDim.x) {
+    const float gq = grad[q];
+    const float mq = 0.9f * m[q] + 0.1f * gq;
+    const float vq = 0.999f * v[q] + 0.001f * gq * gq;
+    m[q] = mq;
+    v[q] = vq;
+    w[q] -= lr * (mq / c1) / (sqrtf(vq / c2) + 1e-8f);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    *loss = grad[kParams] / (float)batch;
+    *step = t;
+  }
+}
+
+}  // namespace
+
+struct pw_closure {
+  float *w = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr, *partial = nullptr, *loss = nullptr;
+  uint32_t *frag = nullptr, *step = nullptr;
+  float *X = nullptr, *Y = nullptr;
+  uint64_t n = 0, cap = 0;
+  uint32_t partial_blocks = 0;
+  cudaStream_t stream = nullptr;
+};
+
+namespace {
+
+size_t train_smem() {
+  return sizeof(float) * (kParams + 3 + kTrainThreads * (kIn + 4 * kHidden + 2));
+}
+
+int ensure_partials(pw_closure *c, uint32_t blocks) {
+  if (blocks <= c->partial_blocks) return PW_OK;
+  cudaFree(c->partial);
+  c->partial = nullptr;
+  c->partial_blocks = 0;
+  PW_TRY(cudaMalloc(&c->partial, (size_t)blocks * (kParams + 1) * sizeof(float)));
+  c->partial_blocks = blocks;
+  return PW_OK;
+}
+
+int refresh_fragments(pw_closure *c) {
+  build_fragments<<<1, 32, 0, c->stream>>>(c->w, c->frag);
+  PW_TRY(cudaGetLastError());
+  return PW_OK;
+}
+
+}  // namespace
+
+namespace pwclosure_host {
+// The closure step for a domain with an attached closure (pw_domain.cu).
+void launch_closure_step(const StepParams &p, int storage, int op, bool odd, dim3 grid, const uint32_t *frag,
+                         const uint8_t *wall, cudaStream_t s) {
+  const dim3 blk(32, 4);
+#define PW_CL_LAUNCH(ST, OPV)                                                                  \
+  do {                                                                                        \
+    if (odd) closure_step<ST, OPV, true><<<grid, blk, 0, s>>>(p, frag, wall);                 \
+    else closure_step<ST, OPV, false><<<grid, blk, 0, s>>>(p, frag, wall);                    \
+  } while (0)
+  if (op == pw::OP_REG) {
+    if (storage == pw::STORE_F16) PW_CL_LAUNCH(pw::STORE_F16, pw::OP_REG);
+    else if (storage == pw::STORE_BF16) PW_CL_LAUNCH(pw::STORE_BF16, pw::OP_REG);
+    else PW_CL_LAUNCH(pw::STORE_F32, pw::OP_REG);
+  } else {
+    if (storage == pw::STORE_F16) PW_CL_LAUNCH(pw::STORE_F16, pw::OP_TRT);
+    else if (storage == pw::STORE_BF16) PW_CL_LAUNCH(pw::STORE_BF16, pw::OP_TRT);
+    else PW_CL_LAUNCH(pw::STORE_F32, pw::OP_TRT);
+  }
+#undef PW_CL_LAUNCH
+}
+
+int wall_distance_of(const uint32_t *flags, uint32_t nx, uint32_t ny, uint32_t nz, uint8_t *out, cudaStream_t s) {
+  const size_t cells = (size_t)nx * ny * nz;
+  uint8_t *tmp = nullptr;
+  PW_TRY(cudaMalloc(&tmp, cells));
+  dist_init<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(flags, cells, out);
+  int rc = wall_distance(out, tmp, nx, ny, nz, s);
+  cudaStreamSynchronize(s);
+  cudaFree(tmp);
+  return rc;
+}
+
+const uint32_t *fragments(const pw_closure *c) { return c->frag; }
+}  // namespace pwclosure_host
+
+extern "C" {
+
+int pw_closure_create(uint64_t seed, pw_closure **out) {
+  if (!out) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  *out = nullptr;
+  pw_closure *c = new pw_closure();
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&c->w, kParams * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&c->m, kParams * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&c->v, kParams * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&c->grad, (kParams + 1) * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&c->loss, sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&c->frag, 32 * kFragWords * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&c->step, sizeof(uint32_t));
+  if (e != cudaSuccess) {
+    int rc = cuda_status(e, "pw_closure_create");
+    pw_closure_destroy(c);
+    return rc;
+  }
+  // Glorot-uniform hidden layers (seeded), zero biases, zero output layer: the
+  // untrained network outputs c = 0, plain Smagorinsky.
+  std::vector<float> w(kParams, 0.0f);
+  uint64_t state = seed;
+  auto uniform = [&]() {
+    state += 0x9E3779B97F4A7C15ull;
+    uint64_t z = state;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+  };
+  const double a1 = std::sqrt(6.0 / (kIn + kHidden)), a2 = std::sqrt(6.0 / (2 * kHidden));
+  for (int k = 0; k < kHidden * kIn; k++) w[kW1 + k] = (float)(a1 * uniform());
+  for (int k = 0; k < kHidden * kHidden; k++) w[kW2 + k] = (float)(a2 * uniform());
+  e = cudaMemcpy(c->w, w.data(), kParams * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(c->m, 0, kParams * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemset(c->v, 0, kParams * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemset(c->step, 0, sizeof(uint32_t));
+  if (e != cudaSuccess) {
+    int rc = cuda_status(e, "pw_closure_create");
+    pw_closure_destroy(c);
+    return rc;
+  }
+  int rc = refresh_fragments(c);
+  if (rc == PW_OK) rc = cudaStreamSynchronize(c->stream) == cudaSuccess ? PW_OK : PW_ERR_CUDA;
+  if (rc != PW_OK) { pw_closure_destroy(c); return rc; }
+  *out = c;
+  return PW_OK;
+}
+
+void pw_closure_destroy(pw_closure *c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  cudaFree(c->w); cudaFree(c->m); cudaFree(c->v); cudaFree(c->grad); cudaFree(c->loss);
+  cudaFree(c->frag); cudaFree(c->step); cudaFree(c->partial); cudaFree(c->X); cudaFree(c->Y);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  cudaGetLastError();
+  delete c;
+}
+
+int pw_closure_get_params(pw_closure *c, float *out) {
+  if (!c || !out) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  PW_TRY(cudaMemcpyAsync(out, c->w, kParams * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  PW_TRY(cudaStreamSynchronize(c->stream));
+  return PW_OK;
+}
+
+int pw_closure_set_params(pw_closure *c, const float *in) {
+  if (!c || !in) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  for (int k = 0; k < kParams; k++)
+    if (!std::isfinite(in[k])) { set_error("Closure parameters must be finite."); return PW_ERR_INVALID; }
+  PW_TRY(cudaMemcpyAsync(c->w, in, kParams * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  PW_TRY(cudaMemsetAsync(c->m, 0, kParams * sizeof(float), c->stream));
+  PW_TRY(cudaMemsetAsync(c->v, 0, kParams * sizeof(float), c->stream));
+  PW_TRY(cudaMemsetAsync(c->step, 0, sizeof(uint32_t), c->stream));
+  int rc = refresh_fragments(c);
+  if (rc != PW_OK) return rc;
+  PW_TRY(cudaStreamSynchronize(c->stream));
+  return PW_OK;
+}
+
+int pw_closure_eval(pw_closure *c, const float *x, uint32_t count, float *out) {
+  if (!c || (!x && count) || (!out && count)) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  if (!count) return PW_OK;
+  float *dx = nullptr, *dy = nullptr;
+  PW_TRY(cudaMalloc(&dx, (size_t)count * kIn * sizeof(float)));
+  cudaError_t e = cudaMalloc(&dy, (size_t)count * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x, (size_t)count * kIn * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) {
+    eval_kernel<<<(count + 127) / 128, 128, 0, c->stream>>>(c->frag, dx, count, dy);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, dy, (size_t)count * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(dx);
+  cudaFree(dy);
+  if (e != cudaSuccess) return cuda_status(e, "pw_closure_eval");
+  return PW_OK;
+}
+
+int pw_closure_gradients(pw_closure *c, const float *x, const float *y, uint32_t count, float *grad, float *loss) {
+  if (!c || !x || !y || !grad || count == 0) { set_error("NULL argument or no samples"); return PW_ERR_INVALID; }
+  float *dx = nullptr, *dy = nullptr;
+  uint32_t *idx = nullptr;
+  const uint32_t blocks = (count + kTrainThreads - 1) / kTrainThreads;
+  int rc = ensure_partials(c, blocks);
+  if (rc != PW_OK) return rc;
+  PW_TRY(cudaFuncSetAttribute(train_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
+  cudaError_t e = cudaMalloc(&dx, (size_t)count * kIn * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&dy, (size_t)count * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&idx, (size_t)count * sizeof(uint32_t));
+  std::vector<uint32_t> seq(count);
+  for (uint32_t i = 0; i < count; i++) seq[i] = i;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x, (size_t)count * kIn * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dy, y, (size_t)count * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(idx, seq.data(), (size_t)count * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) {
+    train_block<<<blocks, kTrainThreads, train_smem(), c->stream>>>(c->w, dx, dy, count, count, 0, c->step, idx,
+                                                                    c->partial);
+    train_reduce<<<(kParams + 1 + 255) / 256, 256, 0, c->stream>>>(c->partial, blocks, c->grad);
+    e = cudaGetLastError();
+  }
+  std::vector<float> h(kParams + 1);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), c->grad, (kParams + 1) * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(dx); cudaFree(dy); cudaFree(idx);
+  if (e != cudaSuccess) return cuda_status(e, "pw_closure_gradients");
+  std::copy(h.begin(), h.begin() + kParams, grad);
+  if (loss) *loss = h[kParams] / (float)count;
+  return PW_OK;
+}
+
+int pw_closure_dataset_clear(pw_closure *c) {
+  if (!c) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  c->n = 0;
+  return PW_OK;
+}
+
+int pw_closure_dataset_reserve(pw_closure *c, uint64_t capacity) {
+  if (!c) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  if (capacity <= c->cap) return PW_OK;
+  float *nx = nullptr, *ny = nullptr;
+  PW_TRY(cudaMalloc(&nx, capacity * kIn * sizeof(float)));
+  cudaError_t e = cudaMalloc(&ny, capacity * sizeof(float));
+  if (e == cudaSuccess && c->n) e = cudaMemcpy(nx, c->X, c->n * kIn * sizeof(float), cudaMemcpyDeviceToDevice);
+  if (e == cudaSuccess && c->n) e = cudaMemcpy(ny, c->Y, c->n * sizeof(float), cudaMemcpyDeviceToDevice);
+  if (e != cudaSuccess) { cudaFree(nx); cudaFree(ny); return cuda_status(e, "pw_closure_dataset_reserve"); }
+  cudaFree(c->X); cudaFree(c->Y);
+  c->X = nx; c->Y = ny; c->cap = capacity;
+  return PW_OK;
+}
+
+int pw_closure_dataset_write(pw_closure *c, const float *x, const float *y, uint64_t count) {
+  if (!c || (count && (!x || !y))) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  int rc = pw_closure_dataset_reserve(c, count ? count : 1);
+  if (rc != PW_OK) return rc;
+  if (count) {
+    PW_TRY(cudaMemcpy(c->X, x, count * kIn * sizeof(float), cudaMemcpyHostToDevice));
+    PW_TRY(cudaMemcpy(c->Y, y, count * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  c->n = count;
+  return PW_OK;
+}
+
+int pw_closure_dataset_size(const pw_closure *c, uint64_t *n) {
+  if (!c || !n) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  *n = c->n;
+  return PW_OK;
+}
+
+int pw_closure_dataset_read(pw_closure *c, uint64_t first, uint64_t count, float *x, float *y) {
+  if (!c || (count && (!x || !y))) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  if (first + count > c->n) { set_error("Dataset range beyond its %llu samples.", (unsigned long long)c->n); return PW_ERR_INVALID; }
+  if (!count) return PW_OK;
+  PW_TRY(cudaMemcpy(x, c->X + first * kIn, count * kIn * sizeof(float), cudaMemcpyDeviceToHost));
+  PW_TRY(cudaMemcpy(y, c->Y + first, count * sizeof(float), cudaMemcpyDeviceToHost));
+  return PW_OK;
+}
+
+// Append the samples of a fine domain's latest macros (the last step must have
+// written them) at the given coarse molecular viscosity.
+int pw_closure_dataset_add(pw_closure *c, pw_domain *fine, double nu0_coarse, uint64_t *added) {
+  if (!c || !fine) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  uint32_t nx, ny, nz;
+  domain_dims(fine, &nx, &ny, &nz);
+  if (nx % 2 || ny % 2 || nz % 2 || nx < 10 || ny < 4 || nz < 4) {
+    set_error("The fine grid must have even dimensions of at least 10 x 4 x 4.");
+    return PW_ERR_INVALID;
+  }
+  if (!(nu0_coarse > 0.0) || !std::isfinite(nu0_coarse)) { set_error("The coarse viscosity must be positive."); return PW_ERR_INVALID; }
+  void *macros = nullptr, *flags = nullptr, *stream = nullptr;
+  int rc = pw_domain_buffers(fine, &macros, &flags, &stream);
+  if (rc != PW_OK) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  const uint32_t cx = nx / 2, cy = ny / 2, cz = nz / 2;
+  const size_t nc = (size_t)cx * cy * cz;
+  float *co = nullptr;
+  uint8_t *solid = nullptr, *dist = nullptr, *tmp = nullptr;
+  uint32_t *counts = nullptr;
+  const uint32_t nblk = (uint32_t)((nc + kScanBlock - 1) / kScanBlock);
+  cudaError_t e = cudaMalloc(&co, 10 * nc * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&solid, nc);
+  if (e == cudaSuccess) e = cudaMalloc(&dist, nc);
+  if (e == cudaSuccess) e = cudaMalloc(&tmp, nc);
+  if (e == cudaSuccess) e = cudaMalloc(&counts, (nblk + 1) * sizeof(uint32_t));
+  uint32_t total = 0;
+  float u_in = 0.0f;
+  if (e == cudaSuccess) {
+    pw::StepParams p = member_params(fine, 2, 0);
+    u_in = p.u_in;
+    coarsen_kernel<<<(unsigned)((nc + 255) / 256), 256, 0, s>>>((const float4 *)macros, (const uint32_t *)flags, nx, ny,
+                                                                 nz, co, solid);
+    dist_from_solid<<<(unsigned)((nc + 255) / 256), 256, 0, s>>>(solid, nc, dist);
+    rc = wall_distance(dist, tmp, cx, cy, cz, s);
+    sample_count<<<nblk, kScanBlock, 0, s>>>(co, dist, cx, cy, cz, (float)nu0_coarse, u_in, counts);
+    scan_counts<<<1, kScanBlock, 0, s>>>(counts, nblk, counts + nblk);
+    e = cudaMemcpyAsync(&total, counts + nblk, 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  if (e == cudaSuccess && rc == PW_OK) {
+    const uint64_t need = c->n + total;
+    if (need > c->cap) rc = pw_closure_dataset_reserve(c, std::max<uint64_t>(need, c->cap * 2));
+  }
+  if (e == cudaSuccess && rc == PW_OK) {
+    sample_write<<<nblk, kScanBlock, 0, s>>>(co, dist, cx, cy, cz, (float)nu0_coarse, u_in, counts, c->n, c->cap,
+                                             c->X, c->Y);
+    e = cudaStreamSynchronize(s);
+  }
+  cudaFree(co); cudaFree(solid); cudaFree(dist); cudaFree(tmp); cudaFree(counts);
+  if (e != cudaSuccess) return cuda_status(e, "pw_closure_dataset_add");
+  if (rc != PW_OK) return rc;
+  c->n += total;
+  if (added) *added = total;
+  return PW_OK;
+}
+
+// Adam over `steps` minibatches of `batch` samples drawn by a seeded hash from
+// the dataset; first and last batch losses (mean squared error of c).
+int pw_closure_train(pw_closure *c, uint32_t steps, uint32_t batch, float lr, uint64_t seed, float *loss_first,
+                     float *loss_last) {
+  if (!c || steps == 0 || batch == 0 || !(lr > 0.0f)) { set_error("Training needs steps, a batch and a positive rate."); return PW_ERR_INVALID; }
+  if (c->n == 0) { set_error("The closure dataset is empty."); return PW_ERR_INVALID; }
+  const uint32_t blocks = (batch + kTrainThreads - 1) / kTrainThreads;
+  int rc = ensure_partials(c, blocks);
+  if (rc != PW_OK) return rc;
+  PW_TRY(cudaFuncSetAttribute(train_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
+  auto one = [&](cudaStream_t s) {
+    train_block<<<blocks, kTrainThreads, train_smem(), s>>>(c->w, c->X, c->Y, c->n, batch, seed, c->step, nullptr,
+                                                            c->partial);
+    train_reduce<<<(kParams + 1 + 255) / 256, 256, 0, s>>>(c->partial, blocks, c->grad);
+    train_adam<<<1, 1024, 0, s>>>(c->w, c->m, c->v, c->grad, c->step, lr, batch, c->loss);
+  };
+  one(c->stream);
+  PW_TRY(cudaGetLastError());
+  if (loss_first) PW_TRY(cudaMemcpyAsync(loss_first, c->loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  // the rest as replays of a captured 100-step graph
+  uint32_t done = 1;
+  const uint32_t chunk = 100;
+  cudaGraphExec_t exec = nullptr;
+  if (steps - done >= chunk) {
+    cudaStream_t cap;
+    PW_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      for (uint32_t k = 0; k < chunk; k++) one(cap);
+      if (cudaStreamEndCapture(cap, &graph) == cudaSuccess && graph) {
+        if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) exec = nullptr;
+        cudaGraphDestroy(graph);
+      }
+    }
+    cudaStreamDestroy(cap);
+    cudaGetLastError();
+  }
+  while (exec && steps - done >= chunk) {
+    if (cudaGraphLaunch(exec, c->stream) != cudaSuccess) break;
+    done += chunk;
+  }
+  if (exec) cudaGraphExecDestroy(exec);
+  for (; done < steps; done++) one(c->stream);
+  PW_TRY(cudaGetLastError());
+  if (loss_last) PW_TRY(cudaMemcpyAsync(loss_last, c->loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  rc = refresh_fragments(c);
+  if (rc != PW_OK) return rc;
+  PW_TRY(cudaStreamSynchronize(c->stream));
+  return PW_OK;
+}
+
+}  // extern "C"

@@ -182,6 +182,8 @@ struct pw_domain {
   uint32_t *edges = nullptr;      // edge cells in ascending order
   uint32_t edge_count = 0;
   dim3 plain_grid;                // the cell grid, or empty when no plain position exists
+  const uint32_t *closure_frag = nullptr;  // attached learned closure (its weight fragments)
+  uint8_t *wall_dist = nullptr;   // cells to the nearest wall, for the closure's inputs
   bool tiled = false;             // TMA-staged row tiles
   uint32_t rows_per_tile = 0;
   unsigned tile_blocks = 0;
@@ -246,9 +248,14 @@ void enqueue_step(pw_domain *d, uint64_t step, float u_in, int write_macro) {
                              d->tile_smem, d->stream);
   else if (d->desc.strict)
     pwstrict::launch_step(p, d->desc.storage, d->desc.op, d->desc.les, odd, d->grid, d->stream);
-  else
+  else if (d->closure_frag)
+    pwclosure_host::launch_closure_step(p, d->desc.storage, d->desc.op, odd, d->grid, d->closure_frag, d->wall_dist,
+                                        d->stream);
+  else if (d->split)
     pwfast::launch_step_split(p, d->desc.storage, d->desc.op, d->desc.les, odd, d->plain_grid, d->edges,
                               d->edge_count, d->stream);
+  else
+    pwfast::launch_step(p, d->desc.storage, d->desc.op, d->desc.les, odd, d->grid, d->stream);
 }
 
 // rampFactor (gpu-solver.ts:119-123) and the f32 rounding of packSolverParams.
@@ -269,8 +276,9 @@ int launch_init(pw_domain *d) {
   else if (d->tiled)
     pwfast::launch_init_lin(p, d->plane[1], d->partials[1], d->desc.storage, d->tile_blocks,
                             d->rows_per_tile * d->nx, d->stream);
-  else if (d->desc.strict)
-    pwstrict::launch_init(p, d->plane[1], d->partials[1], d->desc.storage, d->grid, d->stream);
+  else if (d->desc.strict || !d->split)
+    (d->desc.strict ? pwstrict::launch_init : pwfast::launch_init)(p, d->plane[1], d->partials[1], d->desc.storage,
+                                                                   d->grid, d->stream);
   else {
     // the edge list's blocks own the partials: initialise the state, then take
     // both parities' partials of the start state in that mapping
@@ -512,6 +520,7 @@ void pw_domain_destroy(pw_domain *d) {
   cudaFree(d->flags); cudaFree(d->special); cudaFree(d->partials[0]); cudaFree(d->partials[1]);
   cudaFree(d->force_dev); cudaFree(d->status_dev); cudaFree(d->totals_dev); cudaFree(d->scratch);
   cudaFree(d->edges);
+  cudaFree(d->wall_dist);
   cudaFreeHost(d->force_host); cudaFreeHost(d->status_host);
   cudaEventDestroy(d->force_event);
   cudaStreamDestroy(d->stream);
@@ -638,9 +647,12 @@ static int write_pops(pw_domain *d, const void *in, int mode) {
   } else if (d->tiled) {
     pwfast::launch_write(p, odd, mode, d->scratch, d->desc.storage, d->grid, d->stream);
     pwfast::launch_refresh_lin(p, odd, d->desc.storage, d->tile_blocks, d->rows_per_tile * d->nx, d->stream);
-  } else {
+  } else if (d->split) {
     pwfast::launch_write(p, odd, mode, d->scratch, d->desc.storage, d->grid, d->stream);
     pwfast::launch_refresh_edges(p, odd, d->desc.storage, d->edges, d->edge_count, d->stream);
+  } else {
+    pwfast::launch_write(p, odd, mode, d->scratch, d->desc.storage, d->grid, d->stream);
+    pwfast::launch_refresh(p, odd, d->desc.storage, d->grid, d->stream);
   }
   PW_TRY(cudaStreamSynchronize(d->stream));
   return PW_OK;
@@ -770,3 +782,35 @@ pw::StepParams member_params(const pw_domain *d, uint64_t step, int write_macro)
 }
 void member_advance(pw_domain *d, uint64_t n) { d->steps += n; }
 }  // namespace pwhost
+
+extern "C" int pw_closure_attach(pw_domain *d, const pw_closure *c) {
+  if (!alive(d)) return PW_ERR_INVALID;
+  if (c) {
+    if (d->desc.strict || d->tiled || !d->desc.les) {
+      set_error("A closure needs an LES domain of the fast build's one-cell-per-thread path.");
+      return PW_ERR_INVALID;
+    }
+    if (!d->wall_dist) {
+      PW_TRY(cudaMalloc(&d->wall_dist, d->cells));
+      int rc = pwclosure_host::wall_distance_of(d->flags, d->nx, d->ny, d->nz, d->wall_dist, d->stream);
+      if (rc != PW_OK) return rc;
+    }
+    d->closure_frag = pwclosure_host::fragments(c);
+    d->split = false;
+    d->nblocks = (size_t)d->grid.x * d->grid.y * d->grid.z;
+  } else {
+    if (!d->closure_frag) return PW_OK;
+    d->closure_frag = nullptr;
+    d->split = true;
+    d->nblocks = d->edge_count ? (d->edge_count + pw::kBlockX * pw::kBlockY - 1) / (pw::kBlockX * pw::kBlockY) : 1;
+  }
+  drop_graphs(d);
+  PW_TRY(cudaMemsetAsync(d->partials[0], 0, (size_t)d->grid.x * d->grid.y * d->grid.z * 3 * sizeof(double), d->stream));
+  PW_TRY(cudaMemsetAsync(d->partials[1], 0, (size_t)d->grid.x * d->grid.y * d->grid.z * 3 * sizeof(double), d->stream));
+  int rc = launch_init(d);
+  if (rc != PW_OK) return rc;
+  d->steps = 0;
+  if (d->force_state == FORCE_ENCODED) d->force_state = FORCE_IDLE;
+  PW_TRY(cudaStreamSynchronize(d->stream));
+  return PW_OK;
+}

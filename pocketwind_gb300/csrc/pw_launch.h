@@ -44,3 +44,13 @@ void launch_refresh_edges(const pw::StepParams &p, int odd_layout, int storage, 
 }
 PW_DECLARE_LAUNCHERS(pwstrict)
 
+
+struct pw_closure;
+// The learned closure's step (pw_closure.cu) for a domain with a closure attached:
+// one cell per thread over the tile grid, network inference on the tensor cores.
+namespace pwclosure_host {
+void launch_closure_step(const pw::StepParams &p, int storage, int op, bool odd, dim3 grid, const uint32_t *frag,
+                         const uint8_t *wall, cudaStream_t s);
+int wall_distance_of(const uint32_t *flags, uint32_t nx, uint32_t ny, uint32_t nz, uint8_t *out, cudaStream_t s);
+const uint32_t *fragments(const pw_closure *c);
+}

@@ -221,11 +221,22 @@ __device__ __forceinline__ void update_ref(const StepParams &p, const float *g, 
 //
 // Pairs k = 1..9 are directions (2k-1, 2k) with velocities
 // x, y, z, x+y, x+z, y+z, x-y, x-z, y-z.
+// A relaxation-time hook of the LES branch: given the Smagorinsky relaxation
+// time and the cell's state, return the relaxation time to use.  NoHook keeps
+// Smagorinsky; the learned closure scales its eddy viscosity.
+struct NoHook {
+  __device__ __forceinline__ float operator()(const StepParams &, float tau_s, float, float, float, float, float,
+                                              float, float, float, float, float) const {
+    return tau_s;
+  }
+};
+
 // Returns the cell's omega+ (binary32), which is finite exactly when the
 // LES relaxation time is.
-template <int OP, bool LES>
+template <int OP, bool LES, class Hook = NoHook>
 __device__ __forceinline__ float update_fast(const StepParams &p, float *g, float &rho, float &vx, float &vy,
-                                             float &vz, const float scale = 1.0f, const float inv_scale = 1.0f) {
+                                             float &vz, const float scale = 1.0f, const float inv_scale = 1.0f,
+                                             const Hook &hook = Hook()) {
   float s[10], d[10];
 #pragma unroll
   for (int k = 1; k <= 9; k++) {
@@ -259,7 +270,7 @@ __device__ __forceinline__ float update_fast(const StepParams &p, float *g, floa
       const float t0 = p.tau0;
       const float norm = q > 0.0f ? q * rsqrtf(q) : 0.0f;
       const float arg = t0 * t0 + p.cs_term * norm * inv;
-      const float tau_plus = 0.5f * (t0 + arg * rsqrtf(arg));
+      const float tau_plus = hook(p, 0.5f * (t0 + arg * rsqrtf(arg)), rho, vx, vy, vz, pxx, pyy, pzz, pxy, pxz, pyz);
       om_p = __fdividef(1.0f, tau_plus);
       om_m = __fdividef(1.0f, p.lambda * __fdividef(1.0f, tau_plus - 0.5f) + 0.5f);
     }
@@ -549,9 +560,10 @@ __device__ __forceinline__ void reduce_force(bool any, double fx, double fy, dou
 // ---------------------------------------------------------------- the step
 // One cell of a step.  ODD: this step reads layout E and writes layout O;
 // otherwise the reverse.  flag is the cell's packed flags (0 for plain fluid).
-template <int ST, int OP, bool LES, bool ODD>
+template <int ST, int OP, bool LES, bool ODD, class Hook = NoHook>
 __device__ __forceinline__ void general_cell(const StepParams &p, uint32_t x, uint32_t y, uint32_t z, uint32_t n,
-                                             uint32_t flag, double &fx, double &fy, double &fz, bool &force_any) {
+                                             uint32_t flag, double &fx, double &fy, double &fz, bool &force_any,
+                                             const Hook &hook = Hook()) {
   using S = Store<ST>;
   using T = typename S::T;
   T *f = reinterpret_cast<T *>(p.f);
@@ -591,7 +603,7 @@ __device__ __forceinline__ void general_cell(const StepParams &p, uint32_t x, ui
     if (LES && (flag >> 3) != 0u) {
       update_ref<OP, LES>(p, g, flag, post, rho, vx, vy, vz);
     } else {
-      update_fast<OP, LES>(p, g, rho, vx, vy, vz);
+      update_fast<OP, LES, Hook>(p, g, rho, vx, vy, vz, 1.0f, 1.0f, hook);
 #pragma unroll
       for (int i = 0; i < 19; i++) post[i] = g[i];
     }

