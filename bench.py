@@ -302,6 +302,84 @@ def batch_leg(steps, sample_steps=200, count=64, peak=None):
     return out
 
 
+def closure_leg(fine_steps, train_steps, threads):
+    """The learned closure: fine 256x128x128 vehicle runs (REG + LES + wall model,
+    FP32) at Re 320, 640 and 1280 from seeded 1% velocity perturbations give
+    2x box-filtered samples from the second half of each run; the network trains
+    for `train_steps` Adam steps (batch 65,536, lr 1e-3); the 128x64x64 grid at
+    Re 640 then runs the same physical time with the closure and with plain
+    Smagorinsky.  Drag coefficients (each grid's frontal area) averaged over the
+    last quarter, and device times of the fine and coarse runs."""
+    import numpy as np
+    from pocketwind_gb300 import cases, forces, solver
+    from pocketwind_gb300.closure import Closure
+    net = Closure(1)
+    out = {"fine_grid": "256x128x128", "coarse_grid": "128x64x64", "fine_steps": fine_steps,
+           "train_steps": train_steps, "batch": 65536, "lr": 1e-3}
+    fine_cd = {}
+    fine_ms = None
+    held = []  # the last snapshot of each Re: held out of training
+    for re in (320.0, 640.0, 1280.0):
+        v = cases.vehicle_case(256)
+        nu_f = 0.05 * v.length_cells / re
+        grid = v.grid()
+        s = solver.GpuSolver.create(v.layout, grid, solver.SolverParams(tau0=0.5 + 3 * nu_f, u_in=0.05, les=True,
+                                                                         operator="reg"))
+        cases.perturbed_start(s, grid, 0.05, 0.01, seed=int(re))
+        half = fine_steps // 2
+        samples = cases.run_drag(s, half)
+        snaps = 4
+        for k in range(snaps):
+            samples += cases.run_drag(s, half // snaps)
+            s.step(1, True)  # a macro step for the snapshot
+            start = net.dataset_size
+            net.add_samples(s, nu_f / 2)
+            if k == snaps - 1:
+                held.append((start, net.dataset_size))
+        if re == 640.0:
+            ms = s.time_steps(200)
+            fine_ms = ms / 200
+            tail = [f.fx for f in samples[-len(samples) // 4:]]
+            fine_cd[re] = float(np.mean(tail)) * forces.cd_per_lattice_force(grid.frontal_cells)
+        s.destroy()
+    x, y = net.dataset()
+    mask = np.zeros(len(y), bool)
+    for a, b in held:
+        mask[a:b] = True
+    net.set_dataset(x[~mask], y[~mask])
+    out["samples_train"], out["samples_held_out"] = int((~mask).sum()), int(mask.sum())
+    first, last = net.train(train_steps, batch=65536, lr=1e-3)
+    out["loss_first"], out["loss_last"] = first, last
+    xh, yh = x[mask], y[mask]
+    out["a_priori_mse_held_out"] = {"closure": float(np.mean((net.eval(xh) - yh) ** 2)),
+                                    "smagorinsky": float(np.mean(yh * yh))}
+    coarse = {}
+    for label, attach in (("closure", True), ("smagorinsky", False)):
+        c = cases.vehicle_case(128)
+        nu_c = 0.05 * c.length_cells / 640.0
+        grid = c.grid()
+        s = solver.GpuSolver.create(c.layout, grid, solver.SolverParams(tau0=0.5 + 3 * nu_c, u_in=0.05, les=True,
+                                                                         operator="reg"))
+        if attach:
+            net.attach(s)
+        cases.perturbed_start(s, grid, 0.05, 0.01, seed=640)
+        samples = cases.run_drag(s, fine_steps // 2)
+        tail = [f.fx for f in samples[-len(samples) // 4:]]
+        cd = float(np.mean(tail)) * forces.cd_per_lattice_force(grid.frontal_cells)
+        ms = s.time_steps(200) / 200
+        coarse[label] = {"cd": cd, "ms_per_step": ms, "finite": bool(np.isfinite(s.macros()).all())}
+        s.destroy()
+    ref = fine_cd[640.0]
+    for label in coarse:
+        coarse[label]["cd_rel_err_vs_fine"] = abs(coarse[label]["cd"] - ref) / abs(ref)
+        # the coarse grid covers the same physical time in half the steps
+        coarse[label]["wall_time_ratio_fine_over_coarse"] = (2 * fine_ms) / coarse[label]["ms_per_step"]
+    out["fine_cd_re640"] = ref
+    out["coarse_re640"] = coarse
+    net.destroy()
+    return out
+
+
 def cell_classes(flags):
     """Cells updated per step by the plain-cell kernels (plain fluid with
     1 <= x <= nx-2, and EQ cells without wall links) and by the edge kernel."""
@@ -336,6 +414,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="profiling runs: skip the end-to-end leg")
     ap.add_argument("--batch-steps", type=int, default=2000,
                     help="steps of the 64-tunnel batched leg (0 skips the leg)")
+    ap.add_argument("--closure-steps", type=int, default=4000,
+                    help="fine-grid steps of the learned-closure leg (0 skips the leg)")
+    ap.add_argument("--closure-train-steps", type=int, default=20000, help="Adam steps of the closure leg")
     ap.add_argument("--accuracy-steps", type=int, default=1000,
                     help="vehicle steps of the accuracy leg against FP64 (0 skips the leg)")
     args = ap.parse_args()
@@ -438,6 +519,8 @@ def main():
                                                       line["storage_sweep"]["f32"]["mlups"], 3)
     if world == 1 and args.batch_steps > 0:
         line["batched_tunnels"] = batch_leg(args.batch_steps, peak=peak)
+    if world == 1 and args.closure_steps > 0:
+        line["learned_closure"] = closure_leg(args.closure_steps, args.closure_train_steps, os.cpu_count() or 1)
     if world == 1 and args.accuracy_steps > 0:
         line["accuracy"] = accuracy_leg(args.accuracy_steps, os.cpu_count() or 1)
     if world == 1 and args.cpu_steps > 0:

@@ -153,3 +153,32 @@ def batch_tunnels(count: int = 64, seed: int = 1, u: float = forces.U_LU) -> Lis
         nu = max(NU_MIN_LU, u * length / re)
         out.append(Tunnel((nx, ny, nz), kind, body, re, 0.5 + 3 * nu, length, note))
     return out
+
+
+# ---------------------------------------------------------------- closure data
+def perturbed_start(solver: GpuSolver, grid: VoxelGrid, u_in: float, amplitude: float = 0.01, seed: int = 1) -> None:
+    """Start a domain from equilibrium at rho 1 and the inflow velocity with a
+    seeded uniform perturbation of `amplitude` * u_in on each component of each
+    fluid cell (walls at rest): the seeded inflow perturbations of the closure's
+    training runs."""
+    import numpy as np
+    cells = grid.nx * grid.ny * grid.nz
+    rng = np.random.default_rng(seed)
+    u = np.empty((3, cells), np.float64)
+    u[0] = u_in
+    u[1:] = 0.0
+    u += amplitude * u_in * rng.uniform(-1.0, 1.0, (3, cells))
+    kind = grid.flags & 7
+    walls = (kind >= 1) & (kind <= 3)
+    u[:, walls] = 0.0
+    cx = np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0])
+    cy = np.array([0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 1, -1])
+    cz = np.array([0, 0, 0, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0, -1, 1, -1, 1])
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+    uu = (u * u).sum(0)
+    g = np.empty((19, cells), np.float32)
+    for i in range(19):
+        cu = cx[i] * u[0] + cy[i] * u[1] + cz[i] * u[2]
+        g[i] = w[i] * (3 * cu + 4.5 * cu * cu - 1.5 * uu)
+    g[:, walls] = 0.0
+    solver.write_populations(g.reshape(-1))

@@ -82,25 +82,34 @@ __global__ void build_fragments(const float *w, uint32_t *frag) {
   o[45] = o[46] = o[47] = 0u;
 }
 
-// The network on the 32 cells of a warp (every lane must call; `x` is this
-// lane's input row, `stage` 256 words of shared memory owned by the warp).
-__device__ float warp_mlp(const uint32_t *frag, const float x[kIn], uint32_t *stage) {
-  const uint32_t lane = threadIdx.x & 31u, g = lane >> 2, t = lane & 3;
-  const uint32_t *fr = frag + lane * kFragWords;
+// This lane's operand fragments and biases, held in registers across cells.
+struct Frag {
   uint32_t w1[8], w2[16], w3[4];
-  float b1[8], b2[8];
+  float b1[8], b2[8], b3;
+};
+
+__device__ __forceinline__ Frag load_frag(const uint32_t *frag) {
+  const uint32_t *fr = frag + (threadIdx.x & 31u) * kFragWords;
+  Frag f;
 #pragma unroll
-  for (int k = 0; k < 8; k++) w1[k] = __ldg(&fr[k]);
+  for (int k = 0; k < 8; k++) f.w1[k] = __ldg(&fr[k]);
 #pragma unroll
-  for (int k = 0; k < 16; k++) w2[k] = __ldg(&fr[8 + k]);
+  for (int k = 0; k < 16; k++) f.w2[k] = __ldg(&fr[8 + k]);
 #pragma unroll
-  for (int k = 0; k < 4; k++) w3[k] = __ldg(&fr[24 + k]);
+  for (int k = 0; k < 4; k++) f.w3[k] = __ldg(&fr[24 + k]);
 #pragma unroll
   for (int k = 0; k < 8; k++) {
-    b1[k] = __uint_as_float(__ldg(&fr[28 + k]));
-    b2[k] = __uint_as_float(__ldg(&fr[36 + k]));
+    f.b1[k] = __uint_as_float(__ldg(&fr[28 + k]));
+    f.b2[k] = __uint_as_float(__ldg(&fr[36 + k]));
   }
-  const float b3 = __uint_as_float(__ldg(&fr[44]));
+  f.b3 = __uint_as_float(__ldg(&fr[44]));
+  return f;
+}
+
+// The network on the 32 cells of a warp (every lane must call; `x` is this
+// lane's input row, `stage` 256 words of shared memory owned by the warp).
+__device__ float warp_mlp(const Frag &F, const float x[kIn], uint32_t *stage) {
+  const uint32_t lane = threadIdx.x & 31u, g = lane >> 2, t = lane & 3;
   // stage the inputs: row `lane`, word k = inputs 2k, 2k+1 (inputs 9..15 are zero)
 #pragma unroll
   for (int k = 0; k < 8; k++) {
@@ -116,8 +125,8 @@ __device__ float warp_mlp(const uint32_t *frag, const float x[kIn], uint32_t *st
     float h[4][4];
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-      h[j][0] = b1[2 * j]; h[j][1] = b1[2 * j + 1]; h[j][2] = b1[2 * j]; h[j][3] = b1[2 * j + 1];
-      mma_bf16(h[j], a, &w1[2 * j]);
+      h[j][0] = F.b1[2 * j]; h[j][1] = F.b1[2 * j + 1]; h[j][2] = F.b1[2 * j]; h[j][3] = F.b1[2 * j + 1];
+      mma_bf16(h[j], a, &F.w1[2 * j]);
     }
     uint32_t a2[2][4];
 #pragma unroll
@@ -129,9 +138,9 @@ __device__ float warp_mlp(const uint32_t *frag, const float x[kIn], uint32_t *st
     }
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-      h[j][0] = b2[2 * j]; h[j][1] = b2[2 * j + 1]; h[j][2] = b2[2 * j]; h[j][3] = b2[2 * j + 1];
-      mma_bf16(h[j], a2[0], &w2[(2 * j) * 2]);
-      mma_bf16(h[j], a2[1], &w2[(2 * j + 1) * 2]);
+      h[j][0] = F.b2[2 * j]; h[j][1] = F.b2[2 * j + 1]; h[j][2] = F.b2[2 * j]; h[j][3] = F.b2[2 * j + 1];
+      mma_bf16(h[j], a2[0], &F.w2[(2 * j) * 2]);
+      mma_bf16(h[j], a2[1], &F.w2[(2 * j + 1) * 2]);
     }
 #pragma unroll
     for (int kt = 0; kt < 2; kt++) {
@@ -140,9 +149,9 @@ __device__ float warp_mlp(const uint32_t *frag, const float x[kIn], uint32_t *st
       a2[kt][2] = pack_bf16(tanh_fast(h[2 * kt + 1][0]), tanh_fast(h[2 * kt + 1][1]));
       a2[kt][3] = pack_bf16(tanh_fast(h[2 * kt + 1][2]), tanh_fast(h[2 * kt + 1][3]));
     }
-    float o[4] = {t == 0 ? b3 : 0.0f, 0.0f, t == 0 ? b3 : 0.0f, 0.0f};
-    mma_bf16(o, a2[0], &w3[0]);
-    mma_bf16(o, a2[1], &w3[2]);
+    float o[4] = {t == 0 ? F.b3 : 0.0f, 0.0f, t == 0 ? F.b3 : 0.0f, 0.0f};
+    mma_bf16(o, a2[0], &F.w3[0]);
+    mma_bf16(o, a2[1], &F.w3[2]);
     out_lo[m] = o[0];
     out_hi[m] = o[2];
   }
@@ -191,36 +200,44 @@ __device__ __forceinline__ void cell_inputs(const StepParams &p, const float *st
   features(s, rho, st[2], st[3], st[4], wall, p.nu, nu_s, p.u_in, x);
 }
 
+// Planes of a row of tiles each block walks (the fragments stay in registers).
+constexpr uint32_t kClosurePlanes = 2;
+
 template <int ST, int OP, bool ODD>
-__global__ void __launch_bounds__(128) closure_step(StepParams p, const uint32_t *frag, const uint8_t *wall_dist) {
+__global__ void __launch_bounds__(128, 4) closure_step(StepParams p, const uint32_t *frag, const uint8_t *wall_dist) {
   using S = pw::Store<ST>;
   using T = typename S::T;
   __shared__ uint32_t stage[4][256];
+  const Frag F = load_frag(frag);
   const uint32_t x = blockIdx.x * 32 + threadIdx.x;
   const uint32_t y = blockIdx.y * 4 + threadIdx.y;
-  const uint32_t z = blockIdx.z;
   const bool in = x < p.nx && y < p.ny;
-  const uint32_t n = in ? x + p.nx * (y + p.ny * z) : 0u;
-  const uint32_t flag = in ? __ldg(&p.flags[n]) : (uint32_t)pw::SOLID;
-  float xin[kIn];
+  const uint32_t z_end = min(p.nz, (blockIdx.z + 1) * kClosurePlanes);
+  for (uint32_t z = blockIdx.z * kClosurePlanes; z < z_end; z++) {
+    const uint32_t n = in ? x + p.nx * (y + p.ny * z) : 0u;
+    const uint32_t flag = in ? __ldg(&p.flags[n]) : (uint32_t)pw::SOLID;
+    float xin[kIn];
 #pragma unroll
-  for (int k = 0; k < kIn; k++) xin[k] = 0.0f;
-  const bool plain = in && flag == pw::FLUID;  // fluid without wall links
-  if (plain) {
-    const T *f = reinterpret_cast<const T *>(p.f);
-    const pwclosure::Nbr b = pwclosure::make_nbr(p, x, y, z);
-    float g[19];
+    for (int k = 0; k < kIn; k++) xin[k] = 0.0f;
+    if (in && flag == pw::FLUID) {  // fluid without wall links
+      const T *f = reinterpret_cast<const T *>(p.f);
+      const pwclosure::Nbr b = pwclosure::make_nbr(p, x, y, z);
+      float g[19];
 #pragma unroll
-    for (int i = 0; i < 19; i++) g[i] = S::decode(f[ODD ? b.pull(i, p.stride) : (uint32_t)i * p.stride + n]);
-    float st[11], rho, vx, vy, vz;
-    pwclosure::update_fast<OP, true, CaptureHook>(p, g, rho, vx, vy, vz, 1.0f, 1.0f, CaptureHook{st});
-    cell_inputs(p, st, (float)wall_dist[n], xin);
+      for (int i = 0; i < 19; i++) g[i] = S::decode(f[ODD ? b.pull(i, p.stride) : (uint32_t)i * p.stride + n]);
+      float st[11], rho, vx, vy, vz;
+      pwclosure::update_fast<OP, true, CaptureHook>(p, g, rho, vx, vy, vz, 1.0f, 1.0f, CaptureHook{st});
+      cell_inputs(p, st, (float)wall_dist[n], xin);
+    }
+    const float c = warp_mlp(F, xin, stage[threadIdx.y]);
+    bool any = false;
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    if (in)
+      pwclosure::general_cell<ST, OP, true, ODD, ClosureHook>(p, x, y, z, n, flag, fx, fy, fz, any, ClosureHook{c});
+    // the partial slot of tile (x block, y block, z), as the cell kernels number them
+    const size_t slot = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * z);
+    pwclosure::reduce_force_at(any, fx, fy, fz, p.partials, slot, threadIdx.x + 32 * threadIdx.y);
   }
-  const float c = warp_mlp(frag, xin, stage[threadIdx.y]);
-  bool any = false;
-  double fx = 0.0, fy = 0.0, fz = 0.0;
-  if (in) pwclosure::general_cell<ST, OP, true, ODD, ClosureHook>(p, x, y, z, n, flag, fx, fy, fz, any, ClosureHook{c});
-  pwclosure::reduce_force(any, fx, fy, fz, p.partials);
 }
 
 // Network outputs for given inputs through the same warp path (tests).
@@ -230,7 +247,7 @@ __global__ void eval_kernel(const uint32_t *frag, const float *xin, uint32_t cou
   float x[kIn];
 #pragma unroll
   for (int k = 0; k < kIn; k++) x[k] = i < count ? xin[(size_t)i * kIn + k] : 0.0f;
-  const float c = warp_mlp(frag, x, stage[threadIdx.x >> 5]);
+  const float c = warp_mlp(load_frag(frag), x, stage[threadIdx.x >> 5]);
   if (i < count) out[i] = c;
 }
 
@@ -559,10 +576,11 @@ namespace pwclosure_host {
 void launch_closure_step(const StepParams &p, int storage, int op, bool odd, dim3 grid, const uint32_t *frag,
                          const uint8_t *wall, cudaStream_t s) {
   const dim3 blk(32, 4);
+  const dim3 g(grid.x, grid.y, (grid.z + kClosurePlanes - 1) / kClosurePlanes);
 #define PW_CL_LAUNCH(ST, OPV)                                                                  \
   do {                                                                                        \
-    if (odd) closure_step<ST, OPV, true><<<grid, blk, 0, s>>>(p, frag, wall);                 \
-    else closure_step<ST, OPV, false><<<grid, blk, 0, s>>>(p, frag, wall);                    \
+    if (odd) closure_step<ST, OPV, true><<<g, blk, 0, s>>>(p, frag, wall);                    \
+    else closure_step<ST, OPV, false><<<g, blk, 0, s>>>(p, frag, wall);                       \
   } while (0)
   if (op == pw::OP_REG) {
     if (storage == pw::STORE_F16) PW_CL_LAUNCH(pw::STORE_F16, pw::OP_REG);
