@@ -8,7 +8,13 @@ way src/geometry/stl.ts:29-41 reads a binary STL (skip the 80-byte header and
 4-byte count; per 50-byte record skip the normal, take nine little-endian
 float32 coordinates).  tests/unit/voxelize/fixtures.ts:5-20 scales this unit
 cube into the boxes the voxelizer tests use.
+
+model_fixtures.json: the reference's mesh-import fixture files
+(tests/fixtures/stl/*.stl, obj/*.obj, 3mf/*.3mf; each under 2 KB), base64, as
+inputs for the importer tests (tests/unit/stl.test.ts, obj/obj.test.ts,
+threemf/threemf.test.ts).
 """
+import base64
 import json
 import struct
 import sys
@@ -35,6 +41,13 @@ def main():
         "positions": positions,
     }, indent=1) + "\n")
     print("wrote cube_binary.json with", count, "triangles")
+    files = {}
+    for sub in ("stl", "obj", "3mf"):
+        for f in sorted((ref / "tests/fixtures" / sub).iterdir()):
+            files[f"{sub}/{f.name}"] = base64.b64encode(f.read_bytes()).decode()
+    (here / "model_fixtures.json").write_text(json.dumps({"source": "tests/fixtures/{stl,obj,3mf}",
+                                                          "files": files}, indent=1) + "\n")
+    print("wrote model_fixtures.json with", len(files), "files")
 
 
 if __name__ == "__main__":
