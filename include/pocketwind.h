@@ -201,6 +201,25 @@ PW_API int pw_inject_nan(pw_domain *dom);
 /* Device buffers for interop (macros: float4 per cell; flags: u32 per cell)
  * and the domain's CUDA stream. */
 PW_API int pw_domain_buffers(pw_domain *dom, void **macros, void **flags, void **stream);
+/* fieldVtkBytes (src/io/field-export.ts:31-33 over writeVtk, src/io/vtk.ts:27-81)
+ * for the macros as last written, formatted on the GPU: the 16 * cells + 25
+ * bytes that follow writeVtk's header (rho as big-endian binary32, a newline,
+ * "VECTORS velocity float\n", velocity * velocity_scale as big-endian binary32
+ * triples, a newline).  velocity_scale is latticeToField's speedMps / U_LU
+ * (field-export.ts:22-29), a positive finite number; capacity is the size of
+ * the host buffer out. */
+PW_API int pw_field_vtk_body(pw_domain *dom, double velocity_scale, void *out, size_t capacity);
+/* Solver-state checkpoint (the reference has none; its resume restarts cases,
+ * scripts/validate.ts).  pw_checkpoint_size gives the blob's byte count;
+ * pw_checkpoint_save writes a header (grid size, storage, operator, parameters,
+ * step count, checksum), the populations in the storage's own codes, the macros
+ * and the force partials; pw_checkpoint_load puts a domain created with the same
+ * description and grid back into that state, so that stepping on from it gives
+ * the same bits as the run that saved it.  Mismatched, truncated or corrupted
+ * blobs are PW_ERR_INVALID and leave the domain as it was. */
+PW_API int pw_checkpoint_size(const pw_domain *dom, size_t *bytes);
+PW_API int pw_checkpoint_save(pw_domain *dom, void *out, size_t capacity);
+PW_API int pw_checkpoint_load(pw_domain *dom, const void *in, size_t size);
 /* Time count steps on the domain's stream with CUDA events; *ms receives the
  * elapsed device time. */
 /* ---- batches: many independent domains stepped together (no reference counterpart;

@@ -77,6 +77,10 @@ SIGNATURES = {
     "pw_guard_check": (_int, [_vp, C.POINTER(C.c_int)]),
     "pw_inject_nan": (_int, [_vp]),
     "pw_domain_buffers": (_int, [_vp, _PP, _PP, _PP]),
+    "pw_field_vtk_body": (_int, [_vp, C.c_double, _vp, _sz]),
+    "pw_checkpoint_size": (_int, [_vp, C.POINTER(_sz)]),
+    "pw_checkpoint_save": (_int, [_vp, _vp, _sz]),
+    "pw_checkpoint_load": (_int, [_vp, _vp, _sz]),
     "pw_time_steps": (_int, [_vp, _u64, C.POINTER(C.c_float)]),
     "pw_profile_steps": (_int, [_vp, _u64, C.POINTER(C.c_float)]),
     "pw_batch_create": (_int, [C.POINTER(_vp), C.c_uint32, C.POINTER(_vp)]),

@@ -814,3 +814,190 @@ extern "C" int pw_closure_attach(pw_domain *d, const pw_closure *c) {
   PW_TRY(cudaStreamSynchronize(d->stream));
   return PW_OK;
 }
+
+// ---------------------------------------------------------------- field export, checkpoint
+namespace {
+
+__device__ __forceinline__ uint32_t big_endian(float v) { return __byte_perm(__float_as_uint(v), 0u, 0x0123u); }
+
+// The bytes of writeVtk (src/io/vtk.ts:56-80) after the header, with latticeToField's
+// velocity scale (src/io/field-export.ts:22-29): rho as big-endian binary32; a newline and
+// "VECTORS velocity float\n" (24 bytes, so the velocity block starts on a word); the
+// velocity triples, each the binary64 product value * scale rounded to binary32; a newline.
+__global__ void vtk_body_kernel(const float4 *macros, size_t cells, double scale, uint32_t *out) {
+  const size_t vel = cells + 6;
+  for (size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x; n < cells; n += (size_t)gridDim.x * blockDim.x) {
+    float4 m = macros[n];
+    out[n] = big_endian(m.x);
+    out[vel + 3 * n] = big_endian((float)((double)m.y * scale));
+    out[vel + 3 * n + 1] = big_endian((float)((double)m.z * scale));
+    out[vel + 3 * n + 2] = big_endian((float)((double)m.w * scale));
+  }
+  if (blockIdx.x == 0 && threadIdx.x < 24) {
+    const char text[25] = "\nVECTORS velocity float\n";
+    reinterpret_cast<char *>(out + cells)[threadIdx.x] = text[threadIdx.x];
+    if (threadIdx.x == 0) reinterpret_cast<char *>(out + vel + 3 * cells)[0] = '\n';
+  }
+}
+
+// Solver-state checkpoint: this header, then the populations (direction-major, in the
+// storage's own codes, read at the saved step's parity), the macros (float4 per cell),
+// and both parities' force partials.  Little-endian; the checksum covers header and payload.
+struct CheckpointHeader {
+  char magic[8];
+  uint32_t version;
+  uint32_t header_bytes;
+  uint32_t nx, ny, nz;
+  int32_t storage, op, les, walls, lateral, strict;
+  uint32_t status;
+  uint64_t steps;
+  uint64_t population_bytes, macro_bytes, partial_bytes;
+  float tau0, u_in;
+  uint32_t ramp_steps, reserved;
+  uint64_t checksum;
+};
+static_assert(sizeof(CheckpointHeader) == 112, "checkpoint header layout");
+constexpr char kCheckpointMagic[8] = {'P', 'W', 'S', 'T', 'A', 'T', 'E', '\0'};
+constexpr uint32_t kCheckpointVersion = 1;
+
+// 64-bit words folded with a multiply-xorshift per word (the tail bytes zero-padded).
+uint64_t fold_words(uint64_t h, const unsigned char *p, size_t bytes) {
+  size_t k = 0;
+  for (; k + 8 <= bytes; k += 8) {
+    uint64_t w;
+    std::memcpy(&w, p + k, 8);
+    h = (h ^ w) * 0x9e3779b97f4a7c15ull;
+    h ^= h >> 29;
+  }
+  if (k < bytes) {
+    uint64_t w = 0;
+    std::memcpy(&w, p + k, bytes - k);
+    h = (h ^ w) * 0x9e3779b97f4a7c15ull;
+    h ^= h >> 29;
+  }
+  return h;
+}
+
+// Checksum of the header (its checksum field taken as zero) and the payload.
+uint64_t checkpoint_checksum(CheckpointHeader h, const unsigned char *payload, size_t bytes) {
+  h.checksum = 0;
+  uint64_t s = fold_words(0x243f6a8885a308d3ull, reinterpret_cast<const unsigned char *>(&h), sizeof h);
+  return fold_words(s, payload, bytes);
+}
+
+CheckpointHeader header_of(const pw_domain *d) {
+  CheckpointHeader h{};
+  std::memcpy(h.magic, kCheckpointMagic, 8);
+  h.version = kCheckpointVersion;
+  h.header_bytes = sizeof(CheckpointHeader);
+  h.nx = d->nx; h.ny = d->ny; h.nz = d->nz;
+  h.storage = d->desc.storage; h.op = d->desc.op; h.les = d->desc.les;
+  h.walls = d->desc.walls; h.lateral = d->desc.lateral; h.strict = d->desc.strict;
+  h.steps = d->steps;
+  h.population_bytes = (uint64_t)19 * d->cells * d->esize;
+  h.macro_bytes = (uint64_t)d->cells * sizeof(float4);
+  h.partial_bytes = (uint64_t)2 * d->nblocks * 3 * sizeof(double);
+  h.tau0 = d->tau0; h.u_in = (float)d->desc.u_in;
+  h.ramp_steps = d->desc.ramp_steps;
+  return h;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pw_field_vtk_body(pw_domain *d, double velocity_scale, void *out, size_t capacity) {
+  if (!alive(d) || !out) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  if (!std::isfinite(velocity_scale) || velocity_scale <= 0) {
+    set_error("speedMps must be a positive finite number.");
+    return PW_ERR_INVALID;
+  }
+  size_t bytes = 16 * d->cells + 25;
+  if (capacity < bytes) { set_error("The output buffer is smaller than the field's VTK body."); return PW_ERR_INVALID; }
+  int rc = ensure_scratch(d);
+  if (rc != PW_OK) return rc;
+  unsigned blocks = (unsigned)std::min<size_t>((d->cells + 255) / 256, (size_t)152 * 16);
+  vtk_body_kernel<<<blocks, 256, 0, d->stream>>>(d->macros, d->cells, velocity_scale,
+                                                 reinterpret_cast<uint32_t *>(d->scratch));
+  PW_TRY(cudaGetLastError());
+  PW_TRY(cudaMemcpyAsync(out, d->scratch, bytes, cudaMemcpyDeviceToHost, d->stream));
+  PW_TRY(cudaStreamSynchronize(d->stream));
+  return PW_OK;
+}
+
+int pw_checkpoint_size(const pw_domain *d, size_t *bytes) {
+  if (!alive(d) || !bytes) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  CheckpointHeader h = header_of(d);
+  *bytes = sizeof(CheckpointHeader) + h.population_bytes + h.macro_bytes + h.partial_bytes;
+  return PW_OK;
+}
+
+int pw_checkpoint_save(pw_domain *d, void *out, size_t capacity) {
+  if (!alive(d) || !out) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  CheckpointHeader h = header_of(d);
+  size_t total = sizeof(CheckpointHeader) + h.population_bytes + h.macro_bytes + h.partial_bytes;
+  if (capacity < total) { set_error("The output buffer is smaller than the checkpoint."); return PW_ERR_INVALID; }
+  unsigned char *base = static_cast<unsigned char *>(out);
+  unsigned char *pops = base + sizeof(CheckpointHeader);
+  int rc = read_pops(d, pops, 1);
+  if (rc != PW_OK) return rc;
+  unsigned char *mac = pops + h.population_bytes;
+  unsigned char *part = mac + h.macro_bytes;
+  PW_TRY(cudaMemcpyAsync(mac, d->macros, h.macro_bytes, cudaMemcpyDeviceToHost, d->stream));
+  PW_TRY(cudaMemcpyAsync(part, d->partials[0], h.partial_bytes / 2, cudaMemcpyDeviceToHost, d->stream));
+  PW_TRY(cudaMemcpyAsync(part + h.partial_bytes / 2, d->partials[1], h.partial_bytes / 2, cudaMemcpyDeviceToHost,
+                         d->stream));
+  PW_TRY(cudaMemcpyAsync(&h.status, d->status_dev, 4, cudaMemcpyDeviceToHost, d->stream));
+  PW_TRY(cudaStreamSynchronize(d->stream));
+  h.checksum = checkpoint_checksum(h, pops, total - sizeof(CheckpointHeader));
+  std::memcpy(base, &h, sizeof h);
+  return PW_OK;
+}
+
+int pw_checkpoint_load(pw_domain *d, const void *in, size_t size) {
+  if (!alive(d) || !in) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  CheckpointHeader h;
+  if (size < sizeof h) { set_error("The checkpoint is truncated."); return PW_ERR_INVALID; }
+  std::memcpy(&h, in, sizeof h);
+  if (std::memcmp(h.magic, kCheckpointMagic, 8) != 0 || h.header_bytes != sizeof h) {
+    set_error("The data is not a solver checkpoint.");
+    return PW_ERR_INVALID;
+  }
+  if (h.version != kCheckpointVersion) { set_error("Unsupported checkpoint version."); return PW_ERR_INVALID; }
+  CheckpointHeader mine = header_of(d);
+  if (h.nx != mine.nx || h.ny != mine.ny || h.nz != mine.nz || h.storage != mine.storage || h.op != mine.op ||
+      h.les != mine.les || h.walls != mine.walls || h.lateral != mine.lateral || h.strict != mine.strict ||
+      h.tau0 != mine.tau0 || h.u_in != mine.u_in || h.ramp_steps != mine.ramp_steps) {
+    set_error("The checkpoint was saved by a solver with another layout or other parameters.");
+    return PW_ERR_INVALID;
+  }
+  if (h.population_bytes != mine.population_bytes || h.macro_bytes != mine.macro_bytes ||
+      h.partial_bytes != mine.partial_bytes) {
+    set_error("The checkpoint's sections do not match this solver's kernel layout.");
+    return PW_ERR_INVALID;
+  }
+  if (h.steps > (1ull << 53)) { set_error("The checkpoint's step count is out of range."); return PW_ERR_INVALID; }
+  size_t total = sizeof h + h.population_bytes + h.macro_bytes + h.partial_bytes;
+  if (size < total) { set_error("The checkpoint is truncated."); return PW_ERR_INVALID; }
+  const unsigned char *pops = static_cast<const unsigned char *>(in) + sizeof h;
+  if (checkpoint_checksum(h, pops, total - sizeof h) != h.checksum) {
+    set_error("The checkpoint's checksum does not match its contents.");
+    return PW_ERR_INVALID;
+  }
+  uint64_t old_steps = d->steps;
+  d->steps = h.steps;
+  int rc = write_pops(d, pops, 1);
+  if (rc != PW_OK) { d->steps = old_steps; return rc; }
+  const unsigned char *mac = pops + h.population_bytes;
+  const unsigned char *part = mac + h.macro_bytes;
+  PW_TRY(cudaMemcpyAsync(d->macros, mac, h.macro_bytes, cudaMemcpyHostToDevice, d->stream));
+  PW_TRY(cudaMemcpyAsync(d->partials[0], part, h.partial_bytes / 2, cudaMemcpyHostToDevice, d->stream));
+  PW_TRY(cudaMemcpyAsync(d->partials[1], part + h.partial_bytes / 2, h.partial_bytes / 2, cudaMemcpyHostToDevice,
+                         d->stream));
+  PW_TRY(cudaMemcpyAsync(d->status_dev, &h.status, 4, cudaMemcpyHostToDevice, d->stream));
+  PW_TRY(cudaStreamSynchronize(d->stream));
+  if (d->force_state == FORCE_ENCODED) d->force_state = FORCE_IDLE;
+  return PW_OK;
+}
+
+}  // extern "C"

@@ -197,6 +197,31 @@ class GpuSolver:
     def inject_nan(self) -> None:
         _lib.check(_lib.load().pw_inject_nan(self._live()), "inject_nan")
 
+    # -------------------------------------------------------------- state export
+    def field_vtk_body(self, velocity_scale: float) -> bytes:
+        """The VTK bytes after writeVtk's header for the macros as last written,
+        velocity scaled by ``velocity_scale`` (pw_field_vtk_body)."""
+        n = 16 * self.cells + 25
+        out = np.empty(n, np.uint8)
+        _lib.check(_lib.load().pw_field_vtk_body(self._live(), float(velocity_scale),
+                                                 out.ctypes.data_as(C.c_void_p), n), "field_vtk_body")
+        return out.tobytes()
+
+    def save_checkpoint(self) -> bytes:
+        """The solver state as a self-checking blob (pw_checkpoint_save)."""
+        n = C.c_size_t()
+        L = _lib.load()
+        _lib.check(L.pw_checkpoint_size(self._live(), C.byref(n)), "checkpoint")
+        out = np.empty(n.value, np.uint8)
+        _lib.check(L.pw_checkpoint_save(self._live(), out.ctypes.data_as(C.c_void_p), n.value), "checkpoint")
+        return out.tobytes()
+
+    def load_checkpoint(self, blob: bytes) -> None:
+        """Restore a state saved by a solver of the same layout and parameters."""
+        a = np.frombuffer(blob, np.uint8)
+        _lib.check(_lib.load().pw_checkpoint_load(self._live(), a.ctypes.data_as(C.c_void_p), a.size),
+                   "load_checkpoint")
+
     def buffers(self):
         m, f, s = C.c_void_p(), C.c_void_p(), C.c_void_p()
         _lib.check(_lib.load().pw_domain_buffers(self._live(), C.byref(m), C.byref(f), C.byref(s)))
