@@ -123,6 +123,17 @@ PW_API int pw_device_count(void);
 PW_API int pw_voxelize(const float *body, uint32_t body_triangles, const float *supports,
                 uint32_t support_triangles, uint32_t nx, uint32_t ny, uint32_t nz,
                 int floor_on, pw_grid **out);
+/* voxelize with opts.linkFractions (voxelize.ts:172-199): link_fractions = 1
+ * measures every wall link's fraction as the reference's default does
+ * (linkFraction, wall-links.ts:53-80; binTriangles / nearestLinkHit /
+ * intersection, triangle-bins.ts:1-162): four-cell triangle bins and one
+ * binary64 Moller-Trumbore segment cast per link from the fluid cell toward
+ * its wall, nearest hit clamped to [1e-3, 1]; FLOOR links and misses keep 1/2
+ * and misses count in pw_grid_stats.missed_links.  link_fractions = 0 is
+ * pw_voxelize. */
+PW_API int pw_voxelize_opts(const float *body, uint32_t body_triangles, const float *supports,
+                            uint32_t support_triangles, uint32_t nx, uint32_t ny, uint32_t nz,
+                            int floor_on, int link_fractions, pw_grid **out);
 
 /* A grid from the reference's packed VoxelGrid arrays (geometry = flags,
  * q offsets, f32 fractions; boundary = boundaryCells), validated like

@@ -54,6 +54,7 @@ SIGNATURES = {
     "pw_version": (C.c_char_p, []),
     "pw_device_count": (_int, []),
     "pw_voxelize": (_int, [_vp, _u32, _vp, _u32, _u32, _u32, _u32, _int, _PP]),
+    "pw_voxelize_opts": (_int, [_vp, _u32, _vp, _u32, _u32, _u32, _u32, _int, _int, _PP]),
     "pw_grid_from_host": (_int, [_u32, _u32, _u32, _vp, _sz, _vp, _sz, _PP]),
     "pw_grid_stats_get": (_int, [_vp, C.POINTER(GridStats)]),
     "pw_grid_read_geometry": (_int, [_vp, _vp, _sz]),

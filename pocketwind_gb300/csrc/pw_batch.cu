@@ -286,6 +286,10 @@ int pw_batch_create(pw_domain *const *members, uint32_t count, pw_batch **out) {
       set_error("Batch members must share storage, collision operator and LES.");
       return PW_ERR_INVALID;
     }
+    if (v.interpolated) {
+      set_error("Batch members must use halfway bounce-back walls.");
+      return PW_ERR_INVALID;
+    }
     if (v.steps != first.steps) { set_error("Batch members must have taken the same number of steps."); return PW_ERR_INVALID; }
     if (v.ramping) { set_error("Batch members must have finished their inlet ramp."); return PW_ERR_INVALID; }
   }

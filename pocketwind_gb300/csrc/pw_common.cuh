@@ -10,6 +10,7 @@
 namespace pw {
 
 enum : uint32_t { FLUID = 0, SOLID = 1, SUPPORT = 2, FLOOR = 3, EQ = 4 };
+constexpr uint32_t NO_Q = 0xffffffffu;  // cell without packed link fractions
 enum : int { STORE_F32 = 0, STORE_F16 = 1, STORE_BF16 = 2 };
 enum : int { OP_TRT = 0, OP_REG = 1 };
 
@@ -161,6 +162,15 @@ struct StepParams {
   // n + ld[i] and stored to element n + st[i] of f, offsets for this step's parity.
   uint32_t ld[19];
   uint32_t st[19];
+  // Interpolated walls (walls.wgsl:6-21); null qoff means halfway bounce-back.
+  // qoff[n]: index of cell n's first wall-link fraction (PW_NO_Q without); q: the
+  // fractions in link-rank order; hist: per link, the cell's own post-collision
+  // code in the link's direction from the latest step (the AA pattern overwrites
+  // that population in place, so the cell keeps a copy).  With interpolated walls
+  // a step's force partials hold the momentum exchange of the state it read.
+  const uint32_t *qoff;
+  const float *q;
+  void *hist;
 };
 
 }  // namespace pw

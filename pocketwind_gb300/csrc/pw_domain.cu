@@ -184,6 +184,10 @@ struct pw_domain {
   dim3 plain_grid;                // the cell grid, or empty when no plain position exists
   const uint32_t *closure_frag = nullptr;  // attached learned closure (its weight fragments)
   uint8_t *wall_dist = nullptr;   // cells to the nearest wall, for the closure's inputs
+  bool interp = false;            // interpolated (Bouzidi) walls
+  uint32_t *qoff = nullptr;       // per cell: first wall-link fraction (interpolated walls)
+  float *qfrac = nullptr;         // wall-link fractions in link-rank order
+  void *hist = nullptr;           // per link: the cell's own latest post-collision code
   bool tiled = false;             // TMA-staged row tiles
   uint32_t rows_per_tile = 0;
   unsigned tile_blocks = 0;
@@ -221,6 +225,14 @@ pw::StepParams params_for(const pw_domain *d, uint64_t step, float u_in, int wri
   p.tau0 = d->tau0; p.omega_plus = d->om_p; p.omega_minus = d->om_m;
   p.write_macro = write_macro;
   p.slip = d->slip;
+  if (d->interp) {
+    // a step evaluates the wall values of the state it reads, so its partials
+    // hold that (previous) state's momentum exchange
+    p.qoff = d->qoff;
+    p.q = d->qfrac;
+    p.hist = d->hist;
+    p.partials = d->partials[par ^ 1];
+  }
   // Per-direction element offsets of the plain cells.  Even steps read slot i
   // and write slot opp(j) of the cell itself; odd steps read slot opp(i) of
   // n - c_i and write slot j of n + c_j.  Every offset is non-negative
@@ -266,6 +278,17 @@ float ramp_speed(const pw_domain *d, uint64_t step) {
   return (float)(d->desc.u_in * factor);
 }
 
+// Interpolated walls: the momentum exchange of the state after `steps` steps into
+// that parity's partials, in the step kernels' slot mapping; refresh also copies
+// each link's own population into hist.
+void interp_state(pw_domain *d, uint64_t steps, int refresh) {
+  pw::StepParams p = params_for(d, steps, d->u_in, 0);
+  int odd = (int)(steps & 1);
+  p.partials = d->partials[odd];
+  if (d->desc.strict) pwstrict::launch_interp_state(p, odd, refresh, d->desc.storage, d->grid, nullptr, 0, d->stream);
+  else pwfast::launch_interp_state(p, odd, refresh, d->desc.storage, d->grid, d->edges, d->edge_count, d->stream);
+}
+
 int launch_init(pw_domain *d) {
   float u0 = d->desc.ramp_steps > 0 ? 0.0f : d->u_in;
   PW_TRY(cudaMemsetAsync(d->f, 0, (size_t)19 * d->stride * d->esize, d->stream));
@@ -286,6 +309,12 @@ int launch_init(pw_domain *d) {
     q.partials = nullptr;
     pwfast::launch_init(q, d->plane[1], nullptr, d->desc.storage, d->grid, d->stream);
     pwfast::launch_refresh_edges(p, 0, d->desc.storage, d->edges, d->edge_count, d->stream);
+    PW_TRY(cudaMemcpyAsync(d->partials[1], d->partials[0], d->nblocks * 3 * sizeof(double),
+                           cudaMemcpyDeviceToDevice, d->stream));
+  }
+  if (d->interp) {
+    // both parities start as the start state's momentum exchange with its wall values
+    interp_state(d, 0, 1);
     PW_TRY(cudaMemcpyAsync(d->partials[1], d->partials[0], d->nblocks * 3 * sizeof(double),
                            cudaMemcpyDeviceToDevice, d->stream));
   }
@@ -385,8 +414,9 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
     return PW_ERR_INVALID;
   }
   if (desc->op != PW_OP_TRT && desc->op != PW_OP_REG) { set_error("Unknown collision operator."); return PW_ERR_INVALID; }
-  if (desc->walls != PW_WALLS_BB) {
-    set_error("Interpolated (Bouzidi) walls are not available in the in-place kernel; use halfway bounce-back.");
+  if (desc->walls != PW_WALLS_BB && desc->walls != PW_WALLS_BOUZIDI) { set_error("Unknown wall rule."); return PW_ERR_INVALID; }
+  if (desc->walls == PW_WALLS_BOUZIDI && (desc->kernel == PW_KERNEL_TILE || desc->lateral != PW_LATERAL_PERIODIC)) {
+    set_error("Interpolated (Bouzidi) walls run with the one-cell-per-thread kernels and periodic lateral faces.");
     return PW_ERR_INVALID;
   }
   // packSolverParams (gpu-solver.ts:94-105)
@@ -457,6 +487,10 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
   if (e == cudaSuccess) e = a.alloc((void **)&d->plane[1], plane_n * sizeof(float4));
   if (e == cudaSuccess) e = a.alloc((void **)&d->flags, cells * 4);
   if (e == cudaSuccess) e = a.alloc((void **)&d->special, ((cells + 31) / 32 + 1) * 4);
+  d->interp = desc->walls == PW_WALLS_BOUZIDI;
+  if (d->interp && e == cudaSuccess) e = a.alloc((void **)&d->qoff, cells * 4);
+  if (d->interp && e == cudaSuccess) e = a.alloc((void **)&d->qfrac, (grid->nfrac ? grid->nfrac : 1) * 4);
+  if (d->interp && e == cudaSuccess) e = a.alloc(&d->hist, (grid->nfrac ? grid->nfrac : 1) * d->esize);
   if (e == cudaSuccess) e = a.alloc((void **)&d->partials[0], d->nblocks * 3 * sizeof(double));
   if (e == cudaSuccess) e = a.alloc((void **)&d->partials[1], d->nblocks * 3 * sizeof(double));
   if (e == cudaSuccess) e = a.alloc((void **)&d->force_dev, 4 * sizeof(double));
@@ -477,6 +511,10 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
   unsigned long long *ff = reinterpret_cast<unsigned long long *>(d->totals_dev);
   unsigned long long none = ~0ull;
   cudaMemcpyAsync(d->flags, grid->flags, cells * 4, cudaMemcpyDeviceToDevice, s);
+  if (d->interp) {
+    cudaMemcpyAsync(d->qoff, grid->qoff, cells * 4, cudaMemcpyDeviceToDevice, s);
+    if (grid->nfrac) cudaMemcpyAsync(d->qfrac, grid->fractions, grid->nfrac * 4, cudaMemcpyDeviceToDevice, s);
+  }
   cudaMemsetAsync(d->partials[0], 0, d->nblocks * 3 * sizeof(double), s);
   cudaMemsetAsync(d->partials[1], 0, d->nblocks * 3 * sizeof(double), s);
   cudaMemsetAsync(d->plane[0], 0, plane_n * sizeof(float4), s);
@@ -521,6 +559,7 @@ void pw_domain_destroy(pw_domain *d) {
   cudaFree(d->force_dev); cudaFree(d->status_dev); cudaFree(d->totals_dev); cudaFree(d->scratch);
   cudaFree(d->edges);
   cudaFree(d->wall_dist);
+  cudaFree(d->qoff); cudaFree(d->qfrac); cudaFree(d->hist);
   cudaFreeHost(d->force_host); cudaFreeHost(d->status_host);
   cudaEventDestroy(d->force_event);
   cudaStreamDestroy(d->stream);
@@ -579,6 +618,7 @@ int pw_step_count(const pw_domain *d, uint64_t *out) {
 int pw_encode_force(pw_domain *d) {
   if (!alive(d)) return PW_ERR_INVALID;
   if (d->force_state != FORCE_IDLE) return PW_OK;  // occupied slot skips the sample
+  if (d->interp) interp_state(d, d->steps, 0);  // the latest state; the last step gave the one before
   force_reduce_kernel<<<1, 256, 0, d->stream>>>(d->partials[0], d->partials[1], d->nblocks, d->force_dev);
   PW_TRY(cudaMemcpyAsync(d->force_host, d->force_dev, 3 * sizeof(double), cudaMemcpyDeviceToHost, d->stream));
   PW_TRY(cudaEventRecord(d->force_event, d->stream));
@@ -638,6 +678,7 @@ static int write_pops(pw_domain *d, const void *in, int mode) {
   PW_TRY(cudaMemcpyAsync(d->scratch, in, bytes, cudaMemcpyHostToDevice, d->stream));
   pw::StepParams p = params_for(d, d->steps, d->u_in, 0);
   int odd = (int)(d->steps & 1);
+  if (d->interp) p.partials = nullptr;  // the state pass below takes the force
   if (d->desc.strict && d->tiled) {
     pwstrict::launch_write(p, odd, mode, d->scratch, d->desc.storage, d->grid, d->stream);
     pwstrict::launch_refresh_lin(p, odd, d->desc.storage, d->tile_blocks, d->rows_per_tile * d->nx, d->stream);
@@ -654,6 +695,7 @@ static int write_pops(pw_domain *d, const void *in, int mode) {
     pwfast::launch_write(p, odd, mode, d->scratch, d->desc.storage, d->grid, d->stream);
     pwfast::launch_refresh(p, odd, d->desc.storage, d->grid, d->stream);
   }
+  if (d->interp) interp_state(d, d->steps, 1);
   PW_TRY(cudaStreamSynchronize(d->stream));
   return PW_OK;
 }
@@ -771,6 +813,7 @@ MemberView member_view(const pw_domain *d) {
   v.nx = d->nx; v.ny = d->ny; v.nz = d->nz;
   v.steps = d->steps;
   v.ramping = d->desc.ramp_steps > 0 && d->steps < d->desc.ramp_steps;
+  v.interpolated = d->interp;
   v.edges = d->edges;
   v.edge_count = d->edge_count;
   v.status = d->status_dev;
@@ -786,8 +829,8 @@ void member_advance(pw_domain *d, uint64_t n) { d->steps += n; }
 extern "C" int pw_closure_attach(pw_domain *d, const pw_closure *c) {
   if (!alive(d)) return PW_ERR_INVALID;
   if (c) {
-    if (d->desc.strict || d->tiled || !d->desc.les) {
-      set_error("A closure needs an LES domain of the fast build's one-cell-per-thread path.");
+    if (d->desc.strict || d->tiled || !d->desc.les || d->interp) {
+      set_error("A closure needs an LES domain with halfway walls on the fast build's one-cell-per-thread path.");
       return PW_ERR_INVALID;
     }
     if (!d->wall_dist) {

@@ -14,6 +14,7 @@
 // thread per cell for the rest; prefix sums give CSR column offsets, q offsets and
 // the boundary list in cell order.
 #include <cuda_runtime.h>
+#include <math_constants.h>
 
 #include <cmath>
 #include <cstdarg>
@@ -327,6 +328,217 @@ static int vote_mesh(const float *d_mesh, uint32_t ntri, uint32_t nx, uint32_t n
   return rc;
 }
 
+// ------------------------------------------------------------------ link fractions
+// binTriangles / nearestLinkHit / intersection (src/geometry/triangle-bins.ts:1-162)
+// and linkFraction (src/geometry/wall-links.ts:53-80) in binary64: four-cell bins
+// of triangle offsets, then one thread per fluid cell casts each wall link's segment
+// from the cell centre toward the wall and keeps the nearest Moller-Trumbore hit.
+// The minimum does not depend on the order of a bin's items, so bins fill with
+// atomics and the fractions match the sequential reference bit for bit.
+constexpr int kBin = 4;
+
+struct DevBins {
+  const float *mesh = nullptr;
+  float *bounds = nullptr;      // 6 per triangle: float lo, hi
+  uint32_t *start = nullptr;    // nbins + 1
+  uint32_t *items = nullptr;    // 9 * triangle per entry
+  int bx = 0, by = 0, bz = 0;
+};
+
+__device__ __forceinline__ void bin_range(const double *lo, const double *hi, const DevBins &B, long *r) {
+  const int dims[3] = {B.bx, B.by, B.bz};
+  for (int a = 0; a < 3; a++) {
+    long mn = (long)floor(lo[a] / kBin), mx = (long)floor(hi[a] / kBin);
+    r[2 * a] = mn < 0 ? 0 : mn;
+    r[2 * a + 1] = mx > dims[a] - 1 ? dims[a] - 1 : mx;
+  }
+}
+
+// pass 0 counts the bins each triangle's box touches, pass 1 files the triangle.
+__global__ void bin_triangles_kernel(DevBins B, uint32_t ntri, uint32_t *count, int pass) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntri) return;
+  const float *p = B.mesh + 9 * (size_t)t;
+  double lo[3], hi[3];
+  for (int a = 0; a < 3; a++) {
+    double x = p[a], y = p[a + 3], z = p[a + 6];
+    lo[a] = fmin(fmin(x, y), z);
+    hi[a] = fmax(fmax(x, y), z);
+  }
+  if (pass == 0)
+    for (int a = 0; a < 3; a++) { B.bounds[6 * t + a] = (float)lo[a]; B.bounds[6 * t + 3 + a] = (float)hi[a]; }
+  long r[6];
+  bin_range(lo, hi, B, r);
+  for (long z = r[4]; z <= r[5]; z++)
+    for (long y = r[2]; y <= r[3]; y++)
+      for (long x = r[0]; x <= r[1]; x++) {
+        size_t k = (size_t)x + (size_t)B.bx * ((size_t)y + (size_t)B.by * (size_t)z);
+        uint32_t slot = atomicAdd(&count[k], 1u);
+        if (pass == 1) B.items[B.start[k] + slot] = 9u * t;
+      }
+}
+
+__global__ void set_u32_kernel(uint32_t *p, uint32_t v) { *p = v; }
+
+// intersection, triangle-bins.ts:60-94: the hit depth t along d, or false.
+__device__ bool segment_hit(const float *p, uint32_t off, const double *o, const double *d, double *t) {
+  const double EPS = 1e-9;
+  double ax = p[off], ay = p[off + 1], az = p[off + 2];
+  double e1x = (double)p[off + 3] - ax, e1y = (double)p[off + 4] - ay, e1z = (double)p[off + 5] - az;
+  double e2x = (double)p[off + 6] - ax, e2y = (double)p[off + 7] - ay, e2z = (double)p[off + 8] - az;
+  double px = d[1] * e2z - d[2] * e2y;
+  double py = d[2] * e2x - d[0] * e2z;
+  double pz = d[0] * e2y - d[1] * e2x;
+  double det = e1x * px + e1y * py + e1z * pz;
+  if (fabs(det) < 2.220446049250313e-16) return false;
+  double tx = o[0] - ax, ty = o[1] - ay, tz = o[2] - az;
+  double u = (tx * px + ty * py + tz * pz) / det;
+  if (u < -EPS || u > 1 + EPS) return false;
+  double qx = ty * e1z - tz * e1y;
+  double qy = tz * e1x - tx * e1z;
+  double qz = tx * e1y - ty * e1x;
+  double v = (d[0] * qx + d[1] * qy + d[2] * qz) / det;
+  if (v < -EPS || u + v > 1 + EPS) return false;
+  double tt = (e2x * qx + e2y * qy + e2z * qz) / det;
+  if (tt >= -EPS && tt <= 1 + EPS) { *t = tt; return true; }
+  return false;
+}
+
+// nearestLinkHit, triangle-bins.ts:136-161.
+__device__ bool nearest_link_hit(const DevBins &B, const double *o, const double *d, double *t) {
+  double lo[3], hi[3];
+  for (int a = 0; a < 3; a++) {
+    double e = o[a] + d[a];
+    lo[a] = o[a] < e ? o[a] : e;
+    hi[a] = o[a] > e ? o[a] : e;
+  }
+  long r[6];
+  bin_range(lo, hi, B, r);
+  double nearest = CUDART_INF;
+  for (long z = r[4]; z <= r[5]; z++)
+    for (long y = r[2]; y <= r[3]; y++)
+      for (long x = r[0]; x <= r[1]; x++) {
+        size_t k = (size_t)x + (size_t)B.bx * ((size_t)y + (size_t)B.by * (size_t)z);
+        for (uint32_t it = B.start[k]; it < B.start[k + 1]; it++) {
+          uint32_t off = B.items[it];
+          const float *bd = B.bounds + 6 * (off / 9);
+          if (!((double)bd[0] <= hi[0] && (double)bd[3] >= lo[0] && (double)bd[1] <= hi[1] &&
+                (double)bd[4] >= lo[1] && (double)bd[2] <= hi[2] && (double)bd[5] >= lo[2]))
+            continue;
+          double tt;
+          if (segment_hit(B.mesh, off, o, d, &tt) && tt < nearest) nearest = tt;
+        }
+      }
+  if (nearest == CUDART_INF) return false;
+  *t = nearest;
+  return true;
+}
+
+// linkFraction per wall link of a fluid cell, in link-rank order from its q offset:
+// FLOOR links keep 1/2; SOLID links cast against the body, SUPPORT links against
+// the supports; a miss keeps 1/2 and counts; hits clamp to [1e-3, 1].
+__global__ void link_fraction_kernel(const uint32_t *flags, const uint32_t *qoff, float *fractions, uint32_t nx,
+                                     uint32_t ny, uint32_t nz, int floor_on, DevBins body, DevBins sup, int has_sup,
+                                     uint32_t *missed) {
+  size_t cell = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t cells = (size_t)nx * ny * nz;
+  if (cell >= cells) return;
+  uint32_t flag = flags[cell];
+  if ((flag >> 3) == 0) return;
+  uint32_t f = qoff[cell];
+  long x = (long)(cell % nx), y = (long)((cell / nx) % ny), z = (long)(cell / ((size_t)nx * ny));
+  uint32_t miss = 0;
+  for (int i = 1; i < 19; i++) {
+    if (!(flag & (1u << (3 + i)))) continue;
+    const int cx = pw::cx_of(i), cy = pw::cy_of(i), cz = pw::cz_of(i);
+    // the wall x - c_i: x bounded, y periodic, z periodic unless a floor bounds it
+    long wx = x - cx, wy = (y - cy + (long)ny) % (long)ny, wz = (z - cz + (long)nz) % (long)nz;
+    size_t wall = (size_t)wx + (size_t)nx * ((size_t)wy + (size_t)ny * (size_t)wz);
+    uint32_t type = flags[wall] & 7u;
+    double q = 0.5;
+    bool hit = true;
+    if (type != pw::FLOOR) {
+      const DevBins *bins = type == pw::SUPPORT ? (has_sup ? &sup : nullptr) : &body;
+      double o[3] = {(double)wx + cx, (double)wy + cy, (double)wz + cz};
+      double d[3] = {(double)-cx, (double)-cy, (double)-cz};
+      double t = 0;
+      hit = bins ? nearest_link_hit(*bins, o, d, &t) : false;
+      q = hit ? t : 0.5;
+    }
+    miss += hit ? 0u : 1u;
+    double c = q < 1 ? q : 1;
+    c = c > 1e-3 ? c : 1e-3;
+    fractions[f++] = (float)c;
+  }
+  if (miss) atomicAdd(missed, miss);
+}
+
+static void free_bins(DevBins &B) {
+  cudaFree(B.bounds); cudaFree(B.start); cudaFree(B.items);
+  B = DevBins();
+}
+
+static int build_bins(const float *d_mesh, uint32_t ntri, uint32_t nx, uint32_t ny, uint32_t nz, DevBins *out,
+                      cudaStream_t s) {
+  DevBins B;
+  B.mesh = d_mesh;
+  B.bx = (int)((nx + kBin - 1) / kBin); B.by = (int)((ny + kBin - 1) / kBin); B.bz = (int)((nz + kBin - 1) / kBin);
+  size_t nb = (size_t)B.bx * B.by * B.bz;
+  uint32_t *count = nullptr;
+  uint64_t total = 0;
+  cudaError_t e = cudaMalloc(&B.bounds, (ntri ? ntri : 1) * 6 * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&B.start, (nb + 1) * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&count, nb * 4);
+  int rc = e == cudaSuccess ? PW_OK : cuda_status(e, "triangle bins");
+  if (rc == PW_OK) {
+    cudaMemsetAsync(count, 0, nb * 4, s);
+    if (ntri) bin_triangles_kernel<<<nblk(ntri, 128), 128, 0, s>>>(B, ntri, count, 0);
+    rc = exclusive_scan(count, B.start, nb, &total, s);
+  }
+  if (rc == PW_OK) {
+    set_u32_kernel<<<1, 1, 0, s>>>(B.start + nb, (uint32_t)total);
+    e = cudaMalloc(&B.items, (total ? total : 1) * 4);
+    if (e != cudaSuccess) rc = cuda_status(e, "triangle bins");
+  }
+  if (rc == PW_OK) {
+    cudaMemsetAsync(count, 0, nb * 4, s);
+    if (ntri) bin_triangles_kernel<<<nblk(ntri, 128), 128, 0, s>>>(B, ntri, count, 1);
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = cuda_status(e, "triangle bins");
+  }
+  cudaFree(count);
+  if (rc != PW_OK) { free_bins(B); return rc; }
+  *out = B;
+  return PW_OK;
+}
+
+// Measured fractions for every wall link of a finished grid (buildWallLinks with
+// measureFractions, wall-links.ts:99-131); sets stats.missed_links.
+static int measure_links(pw_grid *g, const float *d_body, uint32_t nbody, const float *d_sup, uint32_t nsup,
+                         bool has_sup, int floor_on, cudaStream_t s) {
+  DevBins body, sup;
+  int rc = build_bins(d_body, nbody, g->nx, g->ny, g->nz, &body, s);
+  if (rc == PW_OK && has_sup) rc = build_bins(d_sup, nsup, g->nx, g->ny, g->nz, &sup, s);
+  uint32_t *missed = nullptr;
+  uint32_t missed_h = 0;
+  if (rc == PW_OK) {
+    cudaError_t e = cudaMalloc(&missed, 4);
+    if (e == cudaSuccess) e = cudaMemsetAsync(missed, 0, 4, s);
+    if (e == cudaSuccess) {
+      link_fraction_kernel<<<nblk(g->cells, 128), 128, 0, s>>>(g->flags, g->qoff, g->fractions, g->nx, g->ny, g->nz,
+                                                               floor_on, body, sup, has_sup ? 1 : 0, missed);
+      e = cudaMemcpyAsync(&missed_h, missed, 4, cudaMemcpyDeviceToHost, s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = cuda_status(e, "link fractions");
+  }
+  cudaFree(missed);
+  free_bins(body);
+  free_bins(sup);
+  if (rc == PW_OK) g->stats.missed_links = missed_h;
+  return rc;
+}
+
 static bool finite_mesh(const float *m, uint32_t ntri) {
   for (size_t k = 0; k < 9 * (size_t)ntri; k++)
     if (!std::isfinite(m[k])) return false;
@@ -433,6 +645,12 @@ int pw_device_count(void) {
 int pw_voxelize(const float *body, uint32_t body_triangles, const float *supports,
                 uint32_t support_triangles, uint32_t nx, uint32_t ny, uint32_t nz, int floor_on,
                 pw_grid **out) {
+  return pw_voxelize_opts(body, body_triangles, supports, support_triangles, nx, ny, nz, floor_on, 0, out);
+}
+
+int pw_voxelize_opts(const float *body, uint32_t body_triangles, const float *supports,
+                     uint32_t support_triangles, uint32_t nx, uint32_t ny, uint32_t nz, int floor_on,
+                     int link_fractions, pw_grid **out) {
   if (!out) { set_error("out is NULL"); return PW_ERR_INVALID; }
   *out = nullptr;
   if (nx < 2 || ny < 2 || nz < 2) {
@@ -460,8 +678,9 @@ int pw_voxelize(const float *body, uint32_t body_triangles, const float *support
   int rc = PW_OK;
   bool body_closed = true, sup_closed = true;
   cudaError_t e = cudaMalloc(&g->flags, cells * 4);
-  size_t maxtri = body_triangles > support_triangles ? body_triangles : support_triangles;
-  if (e == cudaSuccess) e = cudaMalloc(&d_mesh, (maxtri ? maxtri : 1) * 36);
+  float *d_sup = nullptr;
+  if (e == cudaSuccess) e = cudaMalloc(&d_mesh, (body_triangles ? body_triangles : 1) * 36);
+  if (e == cudaSuccess) e = cudaMalloc(&d_sup, (support_triangles ? support_triangles : 1) * 36);
   if (e != cudaSuccess) rc = cuda_status(e, "pw_voxelize");
   if (rc == PW_OK) {
     cudaMemsetAsync(g->flags, 0, cells * 4, s);
@@ -469,15 +688,18 @@ int pw_voxelize(const float *body, uint32_t body_triangles, const float *support
     rc = vote_mesh(d_mesh, body_triangles, nx, ny, nz, g->flags, pw::SOLID, &body_closed, s);
   }
   if (rc == PW_OK && supports) {
-    if (support_triangles) cudaMemcpyAsync(d_mesh, supports, (size_t)support_triangles * 36, cudaMemcpyHostToDevice, s);
-    rc = vote_mesh(d_mesh, support_triangles, nx, ny, nz, g->flags, pw::SUPPORT, &sup_closed, s);
+    if (support_triangles) cudaMemcpyAsync(d_sup, supports, (size_t)support_triangles * 36, cudaMemcpyHostToDevice, s);
+    rc = vote_mesh(d_sup, support_triangles, nx, ny, nz, g->flags, pw::SUPPORT, &sup_closed, s);
   }
   if (rc == PW_OK) {
     boundary_kernel<<<nblk(cells), 256, 0, s>>>(g->flags, nx, ny, nz, floor_on);
     rc = finish_grid(g, floor_on, body_closed, sup_closed, s);
   }
+  if (rc == PW_OK && link_fractions && g->nfrac)
+    rc = measure_links(g, d_mesh, body_triangles, d_sup, support_triangles, supports != nullptr, floor_on, s);
   cudaStreamSynchronize(s);
   cudaFree(d_mesh);
+  cudaFree(d_sup);
   cudaStreamDestroy(s);
   if (rc != PW_OK) { delete g; return rc; }
   *out = g;

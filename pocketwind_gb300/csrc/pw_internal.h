@@ -41,6 +41,7 @@ struct MemberView {
   uint32_t nx, ny, nz;
   uint64_t steps;
   bool ramping;              // inlet ramp still in progress
+  bool interpolated;         // interpolated (Bouzidi) walls
   const uint32_t *edges;
   uint32_t edge_count;
   uint32_t *status;

@@ -19,6 +19,10 @@
                       cudaStream_t s);                                                             \
   void launch_totals(const pw::StepParams &p, int odd_layout, double *out, int storage, dim3 grid, \
                      cudaStream_t s);                                                              \
+  /* interpolated walls: force of the latest state into p.partials (grid mapping, or the edge     \
+     list's when list is set), after copying each link's own population to hist when refresh */  \
+  void launch_interp_state(const pw::StepParams &p, int odd_layout, int refresh, int storage,      \
+                           dim3 grid, const uint32_t *list, uint32_t count, cudaStream_t s);       \
   void launch_init_lin(const pw::StepParams &p, float4 *plane_b, double *partials_b, int storage,  \
                        unsigned blocks, uint32_t cpb, cudaStream_t s);                             \
   void launch_refresh_lin(const pw::StepParams &p, int odd_layout, int storage, unsigned blocks,   \

@@ -557,6 +557,55 @@ __device__ __forceinline__ void reduce_force(bool any, double fx, double fy, dou
   reduce_force_at(any, fx, fy, fz, partials, blk, threadIdx.x + BX * threadIdx.y);
 }
 
+// ---------------------------------------------------------------- interpolated walls
+// wall_value (walls.wgsl:6-21) for every wall link of one fluid cell, in link-rank
+// order.  On entry g[i] of a link holds the halfway value f*_j(n) (j = opp(i)) of
+// the state being read, and g[j] holds f*_j(n + c_i) whenever n + c_i is fluid (it
+// is then n's ordinary pull source for j in both parities); own(i, k) gives the
+// cell's own f*_i(n).  Each link's value replaces g[i]; links into SOLID add
+// c_j (f*_j(n) + value) of that state to fx..fz (force.wgsl:20-29).
+template <class Own>
+__device__ __forceinline__ void interpolated_links(const StepParams &p, const Nbr &b, uint32_t n, uint32_t flag,
+                                                   float *g, const Own &own, double &fx, double &fy, double &fz,
+                                                   bool &force_any) {
+  const uint32_t base = __ldg(&p.qoff[n]);
+  uint32_t k = base;
+#pragma unroll
+  for (int i = 1; i < 19; i++) {
+    if (!(flag & (1u << (3 + i)))) continue;
+    const int j = opp_of(i);
+    const float reflected = g[i];
+    float value = reflected;
+    if (base != NO_Q) {
+      const float q = __ldg(&p.q[k]);
+      if (q != 0.5f) {
+        if (q < 0.5f) {
+          const uint32_t second = b.at(cx_of(i), cy_of(i), cz_of(i));
+          if ((__ldg(&p.flags[second]) & 7u) == FLUID) value = 2.0f * q * reflected + (1.0f - 2.0f * q) * g[j];
+        } else {
+          value = (reflected + (2.0f * q - 1.0f) * own(i, k)) / (2.0f * q);
+        }
+      }
+      k++;
+    }
+    const uint32_t w = b.at(-cx_of(i), -cy_of(i), -cz_of(i));
+    if ((__ldg(&p.flags[w]) & 7u) == SOLID) {
+      double term = (double)(reflected + value);
+      fx += (double)cx_of(j) * term;
+      fy += (double)cy_of(j) * term;
+      fz += (double)cz_of(j) * term;
+      force_any = true;
+    }
+    g[i] = value;
+  }
+}
+
+template <int ST>
+struct OwnFromHist {
+  const typename Store<ST>::T *hist;
+  __device__ __forceinline__ float operator()(int, uint32_t k) const { return Store<ST>::decode(hist[k]); }
+};
+
 // ---------------------------------------------------------------- the step
 // One cell of a step.  ODD: this step reads layout E and writes layout O;
 // otherwise the reverse.  flag is the cell's packed flags (0 for plain fluid).
@@ -597,6 +646,9 @@ __device__ __forceinline__ void general_cell(const StepParams &p, uint32_t x, ui
       }
       g[i] = S::decode(f[src]);
     }
+    if (p.qoff != nullptr && (flag >> 3) != 0u)
+      interpolated_links(p, b, n, flag, g, OwnFromHist<ST>{reinterpret_cast<const T *>(p.hist)}, fx, fy, fz,
+                         force_any);
 #if PW_STRICT
     update_ref<OP, LES>(p, g, flag, post, rho, vx, vy, vz);
 #else
@@ -623,7 +675,17 @@ __device__ __forceinline__ void general_cell(const StepParams &p, uint32_t x, ui
     else dst = (uint32_t)opp_of(j) * S_ + n;
     f[dst] = code[j];
   }
-  if (flag >> 3) {
+  if (p.qoff != nullptr && (flag >> 3) != 0u) {
+    // keep this step's f*_i(n) of every wall link for the next step's wall values
+    const uint32_t base = __ldg(&p.qoff[n]);
+    if (base != NO_Q) {
+      T *hist = reinterpret_cast<T *>(p.hist);
+      uint32_t k = base;
+#pragma unroll
+      for (int i = 1; i < 19; i++)
+        if (flag & (1u << (3 + i))) hist[k++] = code[i];
+    }
+  } else if (flag >> 3) {
     // SOLID links add 2 c_j g*_j to the drag (force.wgsl:20-29, halfway walls).
 #pragma unroll
     for (int i = 1; i < 19; i++) {
@@ -1149,6 +1211,70 @@ __global__ void __launch_bounds__(NTHREADS) aa_refresh_edges(StepParams p, int o
 }
 #endif
 
+// ---------------------------------------------------------------- interpolated walls: state pass
+// The momentum exchange of the latest state with interpolated walls, as the next
+// step will evaluate its wall values (force.wgsl:20-29 over walls.wgsl:6-21), into
+// p.partials; with refresh, each link's f*_i(n) is first copied out of the layout
+// into hist (after an init or a write of the state).
+template <int ST>
+__device__ __forceinline__ void interpolated_state_cell(const StepParams &p, int odd_layout, int refresh, uint32_t x,
+                                                        uint32_t y, uint32_t z, double &fx, double &fy, double &fz,
+                                                        bool &any) {
+  using S = Store<ST>;
+  using T = typename S::T;
+  const T *f = reinterpret_cast<const T *>(p.f);
+  const uint32_t n = x + p.nx * (y + p.ny * z);
+  const uint32_t flag = __ldg(&p.flags[n]);
+  if ((flag & 7u) != FLUID || (flag >> 3) == 0u) return;
+  const Nbr b = make_nbr(p, x, y, z);
+  const uint32_t S_ = p.stride;
+  T *hist = reinterpret_cast<T *>(p.hist);
+  const uint32_t base = __ldg(&p.qoff[n]);
+  if (refresh && base != NO_Q) {
+    uint32_t k = base;
+#pragma unroll
+    for (int i = 1; i < 19; i++)
+      if (flag & (1u << (3 + i))) hist[k++] = f[odd_layout ? slot_of<true>(b, i, S_, n) : slot_of<false>(b, i, S_, n)];
+  }
+  // what the next step reads: it is even after an odd layout, odd after an even one
+  float g[19];
+#pragma unroll
+  for (int i = 0; i < 19; i++) {
+    uint32_t src = odd_layout ? (uint32_t)i * S_ + n : b.pull(i, S_);
+    if (i > 0 && (flag & (1u << (3 + i))))
+      src = odd_layout ? (uint32_t)opp_of(i) * S_ + b.at(-cx_of(i), -cy_of(i), -cz_of(i)) : (uint32_t)i * S_ + n;
+    g[i] = S::decode(f[src]);
+  }
+  interpolated_links(p, b, n, flag, g, OwnFromHist<ST>{hist}, fx, fy, fz, any);
+}
+
+template <int ST>
+__global__ void __launch_bounds__(NTHREADS) aa_interp_state(StepParams p, int odd_layout, int refresh) {
+  const uint32_t x = blockIdx.x * BX + threadIdx.x;
+  const uint32_t y = blockIdx.y * BY + threadIdx.y;
+  const uint32_t z = blockIdx.z;
+  bool any = false;
+  double fx = 0, fy = 0, fz = 0;
+  if (x < p.nx && y < p.ny) interpolated_state_cell<ST>(p, odd_layout, refresh, x, y, z, fx, fy, fz, any);
+  reduce_force(any, fx, fy, fz, p.partials);
+}
+
+#if !PW_STRICT
+template <int ST>
+__global__ void __launch_bounds__(NTHREADS) aa_interp_state_edges(StepParams p, int odd_layout, int refresh,
+                                                                  const uint32_t *list, uint32_t count) {
+  const uint32_t t = blockIdx.x * NTHREADS + threadIdx.x;
+  bool any = false;
+  double fx = 0, fy = 0, fz = 0;
+  if (t < count) {
+    uint32_t x, y, z;
+    cell_coords(p, __ldg(&list[t]), x, y, z);
+    interpolated_state_cell<ST>(p, odd_layout, refresh, x, y, z, fx, fy, fz, any);
+  }
+  reduce_force(any, fx, fy, fz, p.partials);
+}
+#endif
+
 // FP64 mass deviation and momentum of the latest state over non-wall cells.
 template <int ST>
 __global__ void __launch_bounds__(NTHREADS) aa_totals(StepParams p, int odd_layout, double *out) {
@@ -1299,6 +1425,18 @@ void launch_write(const StepParams &p, int odd_layout, int mode, const void *in,
 }
 void launch_refresh(const StepParams &p, int odd_layout, int storage, dim3 g, cudaStream_t s) {
   PW_DISPATCH(storage, (aa_refresh<ST><<<g, dim3(BX, BY), 0, s>>>(p, odd_layout)))
+}
+void launch_interp_state(const StepParams &p, int odd_layout, int refresh, int storage, dim3 g, const uint32_t *list,
+                         uint32_t count, cudaStream_t s) {
+#if !PW_STRICT
+  if (list) {
+    if (!count) return;
+    unsigned blocks = (count + NTHREADS - 1) / NTHREADS;
+    PW_DISPATCH(storage, (aa_interp_state_edges<ST><<<blocks, NTHREADS, 0, s>>>(p, odd_layout, refresh, list, count)))
+    return;
+  }
+#endif
+  PW_DISPATCH(storage, (aa_interp_state<ST><<<g, dim3(BX, BY), 0, s>>>(p, odd_layout, refresh)))
 }
 void launch_totals(const StepParams &p, int odd_layout, double *out, int storage, dim3 g, cudaStream_t s) {
   PW_DISPATCH(storage, (aa_totals<ST><<<g, dim3(BX, BY), 0, s>>>(p, odd_layout, out)))

@@ -96,9 +96,9 @@ def _mesh_array(m) -> tuple:
 
 
 def voxelize(body, supports, layout, floor: bool, link_fractions: bool = False) -> VoxelGrid:
-    """GPU voxelize (voxelize.ts:172); fractions are the halfway value 1/2."""
-    if link_fractions:
-        raise _lib.RangeError("Measured link fractions belong to interpolated walls, which this solver does not run.")
+    """GPU voxelize (voxelize.ts:172); link_fractions measures each wall link's
+    fraction for interpolated walls (wall-links.ts:53-80), otherwise every
+    fraction is the halfway value 1/2."""
     nx, ny, nz = (int(v) for v in layout)
     for v, orig in zip((nx, ny, nz), layout):
         if v != orig or v < 2:
@@ -109,9 +109,9 @@ def voxelize(body, supports, layout, floor: bool, link_fractions: bool = False) 
         b, nb = np.zeros(0, np.float32), 0
     out = C.c_void_p()
     L = _lib.load()
-    _lib.check(L.pw_voxelize(b.ctypes.data_as(C.c_void_p), nb,
-                             None if s is None else s.ctypes.data_as(C.c_void_p), ns,
-                             nx, ny, nz, int(bool(floor)), C.byref(out)), "voxelize")
+    _lib.check(L.pw_voxelize_opts(b.ctypes.data_as(C.c_void_p), nb,
+                                  None if s is None else s.ctypes.data_as(C.c_void_p), ns,
+                                  nx, ny, nz, int(bool(floor)), int(bool(link_fractions)), C.byref(out)), "voxelize")
     return _from_handle(out.value)
 
 

@@ -11,26 +11,29 @@ pytestmark = pytest.mark.gpu
 LAYOUT = (32, 32, 32)
 
 
-def _solver(precision="f16", op="reg", les=True, kernel="auto", lateral="periodic", tau0=0.8, ramp=0):
+def _solver(precision="f16", op="reg", les=True, kernel="auto", lateral="periodic", tau0=0.8, ramp=0, walls="bb",
+            strict=False):
     from pocketwind_gb300 import geometry, solver
-    g, b = blob_grid("bb", LAYOUT)
+    g, b = blob_grid(walls, LAYOUT)
     return solver.GpuSolver.create(LAYOUT, geometry.grid_from_arrays(LAYOUT, g, b),
                                    solver.SolverParams(tau0=tau0, u_in=0.06, les=les, operator=op, precision=precision,
-                                                       kernel=kernel, lateral=lateral, ramp_steps=ramp))
+                                                       kernel=kernel, lateral=lateral, ramp_steps=ramp, walls=walls,
+                                                       strict=strict))
 
 
-@pytest.mark.parametrize("precision,kernel,lateral,first", [
-    ("f16", "auto", "periodic", 41), ("f32", "auto", "free-slip", 40), ("bf16", "tile", "periodic", 13),
-    ("f32", "auto", "periodic", 7)])
-def test_restore_continues_bit_exact(precision, kernel, lateral, first):
+@pytest.mark.parametrize("precision,kernel,lateral,first,walls,strict", [
+    ("f16", "auto", "periodic", 41, "bb", False), ("f32", "auto", "free-slip", 40, "bb", False),
+    ("bf16", "tile", "periodic", 13, "bb", False), ("f32", "auto", "periodic", 7, "bb", False),
+    ("f16", "auto", "periodic", 21, "bouzidi", False), ("f32", "auto", "periodic", 30, "bouzidi", True)])
+def test_restore_continues_bit_exact(precision, kernel, lateral, first, walls, strict):
     ramp = 20 if first == 7 else 0
-    a = _solver(precision, kernel=kernel, lateral=lateral, ramp=ramp)
+    a = _solver(precision, kernel=kernel, lateral=lateral, ramp=ramp, walls=walls, strict=strict)
     a.step(first, True)
     blob = a.save_checkpoint()
     a.step(33, True)
     a.encode_force()
     fa = a.read_force()
-    b = _solver(precision, kernel=kernel, lateral=lateral, ramp=ramp)
+    b = _solver(precision, kernel=kernel, lateral=lateral, ramp=ramp, walls=walls, strict=strict)
     b.step(5)
     b.load_checkpoint(blob)
     assert b.step_count == first

@@ -1,7 +1,8 @@
 """GPU voxelizer parity: the packed geometry and boundary list equal the binary64
-restatement of src/geometry/voxelize.ts + wall-links.ts bit for bit (with the
-halfway fractions of the solver path, linkFractions: false), on the reference's
-own test meshes and on the benchmark bodies."""
+restatement of src/geometry/voxelize.ts + wall-links.ts bit for bit, with the
+halfway fractions of linkFractions: false and with measured link fractions
+(triangle-bins.ts), on the reference's own test meshes and on the benchmark
+bodies."""
 import numpy as np
 import pytest
 
@@ -12,11 +13,11 @@ from tests.shapes import box
 pytestmark = pytest.mark.gpu
 
 
-def _both(body, supports, layout, floor):
+def _both(body, supports, layout, floor, link_fractions=False):
     from pocketwind_gb300.geometry import voxelize
-    g = voxelize(body, supports, layout, floor)
+    g = voxelize(body, supports, layout, floor, link_fractions=link_fractions)
     r = O.voxelize(body.positions, None if supports is None else supports.positions, layout, floor,
-                   link_fractions=False)
+                   link_fractions=link_fractions)
     return g, r
 
 
@@ -36,11 +37,13 @@ CASES = [
 ]
 
 
+@pytest.mark.parametrize("measure", [False, True], ids=["halfway", "measured"])
 @pytest.mark.parametrize("name,make,layout,floor", CASES, ids=[c[0] for c in CASES])
-def test_voxelizer_bit_exact(name, make, layout, floor):
+def test_voxelizer_bit_exact(name, make, layout, floor, measure):
     body, supports = make()
-    g, r = _both(body, supports, layout, floor)
+    g, r = _both(body, supports, layout, floor, measure)
     assert np.array_equal(g.geometry, r.geometry)
+    assert g.missed_links == r.missed_links
     assert np.array_equal(g.boundary_cells, r.boundary_cells)
     assert (g.solid_cells, g.frontal_cells, g.watertight) == (r.solid_cells, r.frontal_cells, r.watertight)
     assert g.blockage == r.blockage

@@ -35,12 +35,12 @@ def _pw():
 
 
 def make_solver(geometry, boundary, layout=LAYOUT, tau0=0.8, u_in=0.06, les=False, op="trt",
-                precision="f32", strict=False, ramp=0, kernel="auto", lateral="periodic"):
+                precision="f32", strict=False, ramp=0, kernel="auto", lateral="periodic", walls="bb"):
     G, S = _pw()
     grid = G.grid_from_arrays(layout, geometry, boundary)
     s = S.GpuSolver.create(layout, grid, S.SolverParams(tau0=tau0, u_in=u_in, les=les, operator=op,
                                                          precision=precision, strict=strict, ramp_steps=ramp,
-                                                         kernel=kernel, lateral=lateral))
+                                                         kernel=kernel, lateral=lateral, walls=walls))
     assert not isinstance(s, Exception)
     return s
 
@@ -439,3 +439,100 @@ def test_free_slip_rejects_the_staged_kernel():
     grid = G.grid_from_arrays(LAYOUT, geometry, boundary)
     with pytest.raises(S.RangeError):
         S.GpuSolver.create(LAYOUT, grid, S.SolverParams(tau0=0.8, u_in=0.06, kernel="tile", lateral="free-slip"))
+
+
+# ---------------------------------------------------------------- interpolated (Bouzidi) walls
+@pytest.mark.parametrize("precision", ["f32", "f16"])
+@pytest.mark.parametrize("op,les", [("trt", False), ("reg", True)])
+def test_strict_blob_bouzidi_is_bit_exact(precision, op, les):
+    """walls.wgsl:6-21 in the in-place kernel: the strict build equals the binary32
+    restatement with A/B buffers bit for bit, populations, macros and the force of
+    the two latest states, on the seeded blob with fractions on both sides of 1/2."""
+    geometry, boundary = blob_grid("bouzidi")
+    gpu = make_solver(geometry, boundary, precision=precision, strict=True, walls="bouzidi", op=op, les=les)
+    ref = O.Wgsl32(32, 32, 32, 0.8, 0.06, geometry, boundary, storage=precision, walls="bouzidi", op=op, les=les,
+                   threads=THREADS)
+    view = np.uint32 if precision == "f32" else np.uint16
+    done = 0
+    for cp in CHECKPOINTS:
+        while done < cp:
+            last = done == cp - 1
+            gpu.step(1, last)
+            ref.step(0.06, last)
+            done += 1
+        assert np.array_equal(gpu.populations_raw().view(view), ref.populations_raw().view(view)), cp
+        assert np.array_equal(gpu.macros().reshape(-1).view(np.uint32), ref.macros().view(np.uint32)), cp
+        gpu.encode_force()
+        f = gpu.read_force()
+        assert f.step == cp
+        assert np.allclose([f.fx, f.fy, f.fz], ref.force(), rtol=1e-12, atol=1e-15), cp
+
+
+def test_fast_blob_bouzidi_matches_fp64_reference():
+    """gpu-vs-cpu.spec.ts TRT + Bouzidi case: normalized max error < 1e-5 from step 0 to 100."""
+    geometry, boundary = blob_grid("bouzidi")
+    gpu = make_solver(geometry, boundary, walls="bouzidi")
+    cpu = O.Cpu64(LAYOUT, 0.8, walls="bouzidi", flags=geometry, equilibrium_state=(1, (0.06, 0, 0)),
+                  threads=THREADS)
+    done = 0
+    for cp in CHECKPOINTS:
+        while done < cp:
+            gpu.step(1, done == cp - 1)
+            cpu.step()
+            done += 1
+        assert norm_err(gpu.populations(), cpu.populations) < 1e-5, cp
+        if cp:
+            assert norm_err(gpu.macros()[:, 1:], cpu.macros()[:, 1:]) < 1e-5, cp
+        gpu.encode_force()
+        f = gpu.read_force()
+        fr = cpu.momentum_exchange()
+        scale = max(F32_EPS, np.abs(fr).max())
+        assert np.abs(np.array([f.fx, f.fy, f.fz]) - fr).max() / scale < 1e-4, cp
+
+
+def test_bouzidi_differs_from_halfway_and_reset_repeats():
+    geometry, boundary = blob_grid("bouzidi")
+    bz = make_solver(geometry, boundary, walls="bouzidi", precision="f16")
+    bb = make_solver(geometry, boundary, walls="bb", precision="f16")
+    bz.step(30, True)
+    bb.step(30, True)
+    a = bz.populations()
+    assert not np.array_equal(a, bb.populations())
+    bz.reset()
+    bz.step(30, True)
+    assert np.array_equal(a, bz.populations())
+
+
+def test_bouzidi_rejects_tile_and_free_slip():
+    from pocketwind_gb300._lib import RangeError
+    geometry, boundary = blob_grid("bouzidi")
+    for kw in (dict(kernel="tile"), dict(lateral="free-slip")):
+        with pytest.raises(RangeError):
+            make_solver(geometry, boundary, walls="bouzidi", **kw)
+
+
+def test_measured_sphere_bouzidi_drag_matches_fp64():
+    """The whole row: measured link fractions from the GPU voxelizer feed the
+    interpolated-wall solver; its drag follows the binary64 reference solver on
+    the same geometry."""
+    from pocketwind_gb300 import geometry as G, meshes, solver as S
+    layout = (64, 32, 32)
+    body = meshes.icosphere((16, 16, 16), 4.3, 3)
+    grid = G.voxelize(body, None, layout, False, link_fractions=True)
+    ref_grid = O.voxelize(body.positions, None, layout, False, link_fractions=True)
+    geo = grid.geometry
+    assert np.array_equal(geo, ref_grid.geometry)
+    q = geo[2 * grid.cells:].view(np.float32)
+    assert q.size and np.any(q < 0.5) and np.any(q > 0.5)
+    nu = 0.05 * 8.6 / 40
+    s = S.GpuSolver.create(layout, grid, S.SolverParams(tau0=0.5 + 3 * nu, u_in=0.05, walls="bouzidi"))
+    cpu = O.Cpu64(layout, 0.5 + 3 * nu, walls="bouzidi", flags=geo, equilibrium_state=(1, (0.05, 0, 0)),
+                  threads=THREADS)
+    for _ in range(4):
+        s.step(50)
+        for _ in range(50):
+            cpu.step()
+        s.encode_force()
+        f = s.read_force()
+        fr = cpu.momentum_exchange()
+        assert abs(f.fx - fr[0]) < 1e-4 * abs(fr[0])
