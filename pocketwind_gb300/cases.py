@@ -38,16 +38,18 @@ class Case:
     average_steps: int
     length_cells: float
     extra: dict = field(default_factory=dict)
+    walls: str = "bb"
 
     def grid(self) -> VoxelGrid:
-        return voxelize(self.body, None, self.layout, self.floor)
+        return voxelize(self.body, None, self.layout, self.floor, link_fractions=self.walls == "bouzidi")
 
     def params(self, precision: str = "f32", strict: bool = False) -> SolverParams:
         return SolverParams(tau0=self.tau0, u_in=self.u_in, les=self.les, operator=self.operator,
-                            precision=precision, strict=strict, lateral=self.lateral)
+                            precision=precision, strict=strict, lateral=self.lateral, walls=self.walls)
 
 
-def sphere_case(lateral: str = "free-slip", nx: int = 96, re: float = 100.0, subdivisions: int = 4) -> Case:
+def sphere_case(lateral: str = "free-slip", nx: int = 96, re: float = 100.0, subdivisions: int = 4,
+                walls: str = "bb") -> Case:
     ny = nz = nx // 2
     diameter = nx / 8
     u = forces.U_LU
@@ -55,7 +57,7 @@ def sphere_case(lateral: str = "free-slip", nx: int = 96, re: float = 100.0, sub
     centre = (nx / 4, ny / 2, nz / 2)
     body = meshes.icosphere(centre, diameter / 2, subdivisions)
     return Case("sphere-re-%g" % re, (nx, ny, nz), body, False, 0.5 + 3 * nu, u, "trt", False, lateral,
-                4000, 1000, diameter, {"re": re, "nu": nu, "diameter": diameter})
+                4000, 1000, diameter, {"re": re, "nu": nu, "diameter": diameter}, walls)
 
 
 def vehicle_case(nx: int = 128, lateral: str = "periodic", steps: int = 20000) -> Case:

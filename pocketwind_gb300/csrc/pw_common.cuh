@@ -63,6 +63,16 @@ __device__ __forceinline__ uint32_t lowbias32(uint32_t bits, uint32_t i, uint32_
 // Odd per-direction multipliers of the fast build's dither hash.
 __host__ __device__ constexpr uint32_t dither_mul(int i) { return (0x9e3779b1u ^ ((uint32_t)i * 0x85ebca6bu)) | 1u; }
 
+// Random bits for encode_pair of two codes of direction i: for each value the
+// high half of its own hash bits * dither_mul(i) + nk (nk = n * 0x9e3779b9 of
+// its cell), so a code's rounding depends on its own value, cell and direction
+// only (as encode_fast's), never on its partner's.
+__device__ __forceinline__ uint32_t pair_dither(float hi, float lo, uint32_t mj, uint32_t nk_hi, uint32_t nk_lo) {
+  const uint32_t h_hi = __float_as_uint(hi) * mj + nk_hi;
+  const uint32_t h_lo = __float_as_uint(lo) * mj + nk_lo;
+  return __byte_perm(h_lo, h_hi, 0x7632u);  // h_lo[31:16] low, h_hi[31:16] high
+}
+
 template <int S> struct Store;
 
 template <> struct Store<STORE_F32> {
@@ -97,6 +107,16 @@ template <> struct Store<STORE_F16> {
     const uint32_t r = bits * mj + nk;
     return __float2half_rz(__uint_as_float(bits + (r >> 19)));
   }
+  // Two codes at once by the hardware's stochastic conversion (cvt.rs, sm_100
+  // family): it adds rbits[28:16] to the 13 bits that hi discards and rbits[12:0]
+  // to those of lo, then truncates: the rule of encode_fast with the dither
+  // supplied.  .satfinite keeps overflow at 65504 and NaN a NaN.  Returns
+  // code(hi) << 16 | code(lo).
+  __device__ __forceinline__ static uint32_t encode_pair(float hi, float lo, uint32_t rbits) {
+    uint32_t d;
+    asm("cvt.rs.satfinite.f16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
+    return d;
+  }
   __device__ __forceinline__ static __half encode(float value, uint32_t i, uint32_t n) {
     float scaled = value * kScale;
     // CUDA's NaN (0x7fffffff) would carry into the sign below and become -0; the
@@ -124,6 +144,13 @@ template <> struct Store<STORE_BF16> {
     const uint32_t bits = __float_as_uint(value);
     const uint32_t r = bits * mj + nk;
     return __float2bfloat16_rz(__uint_as_float(bits + (r >> 16)));
+  }
+  // encode_pair of the f16 codec for bfloat16: rbits[31:16] and rbits[15:0] are
+  // added to the 16 discarded bits of hi and lo.
+  __device__ __forceinline__ static uint32_t encode_pair(float hi, float lo, uint32_t rbits) {
+    uint32_t d;
+    asm("cvt.rs.bf16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
+    return d;
   }
   // The f16 dithering rule applied to the 16 bits bfloat16 discards.
   __device__ __forceinline__ static __nv_bfloat16 encode(float value, uint32_t i, uint32_t n) {

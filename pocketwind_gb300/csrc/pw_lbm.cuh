@@ -804,6 +804,27 @@ __device__ __forceinline__ void eq_cell(const StepParams &p, uint32_t n, uint32_
   }
 }
 
+// The stored codes of one direction of the cell pair in v (.x, .y): 16-bit
+// storages round both with one paired stochastic conversion.
+template <int ST>
+__device__ __forceinline__ void encode_two(float2 v, int j, uint32_t nk, uint32_t nk2, typename Store<ST>::T &a,
+                                           typename Store<ST>::T &b) {
+  using S = Store<ST>;
+  if constexpr (ST == STORE_F32) {
+    a = S::encode_fast(v.x, dither_mul(j), nk);
+    b = S::encode_fast(v.y, dither_mul(j), nk2);
+  } else {
+    const uint32_t w = S::encode_pair(v.y, v.x, pair_dither(v.y, v.x, dither_mul(j), nk2, nk));
+    if constexpr (ST == STORE_F16) {
+      a = __ushort_as_half((unsigned short)(w & 0xffffu));
+      b = __ushort_as_half((unsigned short)(w >> 16));
+    } else {
+      a = __ushort_as_bfloat16((unsigned short)(w & 0xffffu));
+      b = __ushort_as_bfloat16((unsigned short)(w >> 16));
+    }
+  }
+}
+
 // Cells n and n + 32 (x and x + 32 of one row) per thread, the arithmetic in
 // packed pairs and the second cell's elements 32 away from the first's.  ok
 // (bit 0: n, bit 1: n + 32) marks the lanes that are stored: plain cells, and
@@ -856,8 +877,10 @@ __device__ __forceinline__ void plain_pair(const StepParams &p, uint32_t n, uint
 #pragma unroll
     for (int j = 0; j < 19; j++) {
       T *a = f + (n + p.st[j]);
-      if (ok & 1u) a[0] = S::encode_fast(g[j].x, dither_mul(j), nk);
-      if (ok & 2u) a[32] = S::encode_fast(g[j].y, dither_mul(j), nk2);
+      T ca, cb;
+      encode_two<ST>(g[j], j, nk, nk2, ca, cb);
+      if (ok & 1u) a[0] = ca;
+      if (ok & 2u) a[32] = cb;
     }
   } else {
     const uint32_t xa = x, xb = x + 32u;
@@ -865,8 +888,10 @@ __device__ __forceinline__ void plain_pair(const StepParams &p, uint32_t n, uint
     for (int j = 0; j < 19; j++) {
       const uint32_t wa = cx_of(j) < 0 && xa == 0u ? p.nx : (cx_of(j) > 0 && xa + 1u == p.nx ? 0u - p.nx : 0u);
       const uint32_t wb = cx_of(j) > 0 && xb + 1u == p.nx ? 0u - p.nx : 0u;
-      if (ok & 1u) f[n + p.st[j] + wa] = S::encode_fast(g[j].x, dither_mul(j), nk);
-      if (ok & 2u) f[n + 32u + p.st[j] + wb] = S::encode_fast(g[j].y, dither_mul(j), nk2);
+      T ca, cb;
+      encode_two<ST>(g[j], j, nk, nk2, ca, cb);
+      if (ok & 1u) f[n + p.st[j] + wa] = ca;
+      if (ok & 2u) f[n + 32u + p.st[j] + wb] = cb;
     }
   }
   if (p.write_macro) {
@@ -918,6 +943,124 @@ __global__ void __launch_bounds__(NTHREADS) aa_step_fast(StepParams p) {
   const uint32_t z = blockIdx.z + (ODD ? 1u : 0u);
   if (y + (ODD ? 1u : 0u) >= p.ny) return;
   plain_thread<ST, OP, LES, ODD>(p, x, y, z);
+}
+
+// ---------------------------------------------------------------- 16-bit cell pairs
+// The 16-bit storages' plain kernel of even steps: lane t of a warp takes the
+// adjacent cells x0 = 64 r + 2t and x0 + 1 of a 64-cell run r of a row (nx even,
+// so a pair is one aligned 32-bit word of every direction plane).  Even steps
+// touch only the cell's own slots, so each direction is one 32-bit load and
+// one 32-bit store of both cells' codes (whole 128-byte lines per warp), and the
+// store word comes straight out of the paired stochastic conversion.  A word
+// whose two cells are not both stored here (an x-face or wall-link neighbour
+// belongs to the edge kernel) is written half by half.  Odd steps, whose
+// x-shifted directions straddle the word grid, keep the x / x + 32 kernel.
+__device__ __forceinline__ uint32_t ld_word(const void *a) {
+  uint32_t v;
+  asm("ld.global.L2::256B.b32 %0, [%1];" : "=r"(v) : "l"(a));
+  return v;
+}
+__device__ __forceinline__ void st_word(void *a, uint32_t v) {
+  asm volatile("st.global.b32 [%0], %1;" ::"l"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_half(void *a, uint32_t v) {
+  asm volatile("st.global.b16 [%0], %1;" ::"l"(a), "h"((unsigned short)v) : "memory");
+}
+
+template <int ST>
+__device__ __forceinline__ float raw_of_bits(uint32_t b) {
+  if (ST == STORE_F16) return __half2float(__ushort_as_half((unsigned short)b));
+  return __uint_as_float(b << 16);
+}
+
+template <int ST, int OP, bool LES>
+__device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint32_t x, uint32_t y, uint32_t z,
+                                           uint32_t ok, uint32_t eq) {
+  using S = Store<ST>;
+  uint16_t *f = reinterpret_cast<uint16_t *>(p.f);
+  float2 eux = f2(p.u_in), euy = f2(0.f), euz = f2(0.f);
+  if ((eq & 2u) && x + 2u == p.nx) {  // the outlet is the pair's second cell (x even, nx even)
+    const float4 u = p.plane_in[y + p.ny * z];
+    eux.y = u.x; euy.y = u.y; euz.y = u.z;
+  }
+  float2 g[19];
+#pragma unroll
+  for (int i = 0; i < 19; i++) {
+    const uint32_t w = ld_word(f + (n + p.ld[i]));
+    g[i] = make_float2(raw_of_bits<ST>(w & 0xffffu), raw_of_bits<ST>(w >> 16));
+  }
+  float2 rho, vx, vy, vz;
+  const float2 om = update_fast2<OP, LES>(p, g, rho, vx, vy, vz, S::kScale, S::kInvScale, eq, eux, euy, euz);
+  // a non-finite state is stored as NaN, as the reference's GPUs store it
+  if (!(fabsf(rho.x + om.x) < INFINITY)) {
+#pragma unroll
+    for (int j = 0; j < 19; j++) g[j].x = __uint_as_float(0x7fc00000u);
+  }
+  if (!(fabsf(rho.y + om.y) < INFINITY)) {
+#pragma unroll
+    for (int j = 0; j < 19; j++) g[j].y = __uint_as_float(0x7fc00000u);
+  }
+  const uint32_t nk = n * 0x9e3779b9u, nk2 = nk + 0x9e3779b9u;
+  // the outlet's upstream cell (x = nx - 2, the first of its pair) publishes the
+  // velocity of its stored codes
+  const bool pub = (ok & 1u) && x + 2u == p.nx;
+  float mass = 1.0f, mx = 0.f, my = 0.f, mz = 0.f;
+#pragma unroll
+  for (int j = 0; j < 19; j++) {
+    const uint32_t w = S::encode_pair(g[j].y, g[j].x, pair_dither(g[j].y, g[j].x, dither_mul(j), nk2, nk));
+    uint16_t *a = f + (n + p.st[j]);
+    if (ok == 3u) st_word(a, w);
+    else {
+      if (ok & 1u) st_half(a, w & 0xffffu);
+      if (ok & 2u) st_half(a + 1, w >> 16);
+    }
+    if (pub) {
+      const float v = raw_of_bits<ST>(w & 0xffffu) * S::kInvScale;
+      mass += v;
+      mx += (float)cx_of(j) * v;
+      my += (float)cy_of(j) * v;
+      mz += (float)cz_of(j) * v;
+    }
+  }
+  if (pub) {
+    const float inv = __fdividef(1.0f, mass);
+    p.plane_out[y + p.ny * z] = make_float4(mx * inv, my * inv, mz * inv, 0.f);
+  }
+  if (p.write_macro) {
+    const bool bad_a = (ok & ~eq & 1u) && !(rho.x >= 0.5f && rho.x <= 1.5f);
+    const bool bad_b = (ok & ~eq & 2u) && !(rho.y >= 0.5f && rho.y <= 1.5f);
+    if (bad_a || bad_b) atomicOr(p.status, 1u);
+    if (ok & 1u) p.macros[n] = make_float4(rho.x, vx.x, vy.x, vz.x);
+    if (ok & 2u) p.macros[n + 1] = make_float4(rho.y, vx.y, vy.y, vz.y);
+  }
+}
+
+template <int ST, int OP, bool LES>
+__device__ __forceinline__ void pair_thread(const StepParams &p, uint32_t x, uint32_t y, uint32_t z) {
+  if (x >= p.nx) return;
+  const uint32_t n = x + p.nx * (y + p.ny * z);
+  const uint32_t word = __ldg(&p.special[n >> 5]);
+  uint32_t ok = 0u, eq = 0u;
+#pragma unroll
+  for (uint32_t k = 0; k < 2u; k++) {
+    const uint32_t xk = x + k, nk = n + k;
+    if (!((word >> (nk & 31u)) & 1u)) {
+      if (is_plain_position(xk, p.nx)) ok |= 1u << k;
+    } else if (__ldg(&p.flags[nk]) == EQ) {
+      ok |= 1u << k;
+      eq |= 1u << k;
+    }
+  }
+  if (ok) pair_cells<ST, OP, LES>(p, n, x, y, z, ok, eq);
+}
+
+// Even steps, one warp per 64-cell run of a row.
+template <int ST, int OP, bool LES>
+__global__ void __launch_bounds__(NTHREADS) aa_step_pairs(StepParams p) {
+  const uint32_t x = blockIdx.x * (2 * BX) + 2u * threadIdx.x;
+  const uint32_t y = blockIdx.y * BY + threadIdx.y;
+  if (y >= p.ny) return;
+  pair_thread<ST, OP, LES>(p, x, y, blockIdx.z);
 }
 
 // Odd steps on the seam rows: every row of the planes z = 0 and z = nz-1, then
@@ -1354,6 +1497,8 @@ static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *l
                         const cudaEvent_t *ev) {
   if (g.x && g.y && g.z) {
     const unsigned runs = (p.nx + 2 * BX - 1) / (2 * BX);  // 64-cell runs per row
+    // even steps of 16-bit storage with whole 32-bit pairs in a row: the pair kernel
+    const bool pairs = ST != STORE_F32 && (p.nx & 1u) == 0u;
     if (odd) {
       dim3 inner(runs, p.ny > 2u ? (p.ny - 2u + BY - 1u) / BY : 0u, p.nz > 2u ? p.nz - 2u : 0u);
       mark(ev, 0, s);
@@ -1364,7 +1509,13 @@ static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *l
       mark(ev, 3, s);
     } else {
       mark(ev, 0, s);
-      aa_step_fast<ST, OP, LES, false><<<dim3(runs, g.y, g.z), dim3(BX, BY), 0, s>>>(p);
+      if constexpr (ST != STORE_F32) {
+        if (pairs) aa_step_pairs<ST, OP, LES><<<dim3(runs, g.y, g.z), dim3(BX, BY), 0, s>>>(p);
+        else aa_step_fast<ST, OP, LES, false><<<dim3(runs, g.y, g.z), dim3(BX, BY), 0, s>>>(p);
+      } else {
+        (void)pairs;
+        aa_step_fast<ST, OP, LES, false><<<dim3(runs, g.y, g.z), dim3(BX, BY), 0, s>>>(p);
+      }
       mark(ev, 1, s);
       mark(ev, 2, s);
       mark(ev, 3, s);
