@@ -15,9 +15,10 @@ e2e     = the same metric through the public solver API the reference's headless
           runner uses (src/app/case-run.ts:154-169): host mesh -> GPU voxelizer ->
           create -> {step 8, encode force, read force} loop, wall clock, with the
           mesh upload (once) and every force readback inside the timed region.
-roofline: the plain-cell kernels (the two-cell packed-FP32 kernel, and on odd
-          steps its seam-row variant), which update all but the wall-link and
-          x-face cells: algorithmic bytes per cell update B = 2 * 19 * s + 1/8
+roofline: the plain-cell kernels (even steps: the 32-bit cell-pair kernel;
+          odd steps: the two-cell x / x+32 kernel and its seam-row variant), all
+          packed FP32 arithmetic, which update all but the wall-link and x-face
+          cells: algorithmic bytes per cell update B = 2 * 19 * s + 1/8
           (s = 2 bytes; the 1/8 is the bit-packed special mask), achieved =
           their cells * B / their summed CUDA-event time per step, peak =
           measured HBM copy GB/s.  step_roofline repeats it for whole steps.
@@ -219,6 +220,31 @@ def accuracy_leg(steps, threads):
                            "drag_rel_err": abs(fx - rfx) / abs(rfx),
                            "cd": fx * forces.cd_per_lattice_force(grid.frontal_cells),
                            "frontal_cells": grid.frontal_cells}
+    # the same sphere with interpolated walls on measured link fractions (periodic
+    # lateral faces), and halfway walls on that grid for comparison
+    c = cases.sphere_case("periodic", walls="bouzidi")
+    grid = c.grid()
+    row = {"grid": "96x48x48", "storage": "f32", "operator": "trt", "lateral": "periodic",
+           "steps": c.steps, "average_steps": c.average_steps, "frontal_cells": grid.frontal_cells,
+           "missed_links": grid.missed_links}
+    for walls in ("bouzidi", "bb"):
+        p = c.params("f32")
+        p.walls = walls
+        s = GpuSolver.create(c.layout, grid, p)
+        fx, fy, fz = cases.mean_drag(cases.run_drag(s, c.steps), c.steps, c.average_steps)
+        s.destroy()
+        row[walls] = {"fx": fx, "cd": fx * forces.cd_per_lattice_force(grid.frontal_cells)}
+    cpu = O.Cpu64(c.layout, c.tau0, walls="bouzidi", flags=grid.geometry,
+                  equilibrium_state=(1.0, (c.u_in, 0.0, 0.0)), threads=threads)
+    window = []
+    for k in range(8, c.steps + 1, 8):
+        cpu.step(8)
+        if k > c.steps - c.average_steps:
+            window.append(cpu.momentum_exchange()[0])
+    rfx = float(np.mean(window))
+    row["bouzidi"]["fx_fp64"] = rfx
+    row["bouzidi"]["drag_rel_err"] = abs(row["bouzidi"]["fx"] - rfx) / abs(rfx)
+    out["sphere_re100_bouzidi"] = row
     v = cases.vehicle_case(128)
     grid = v.grid()
     cpu = O.Cpu64(v.layout, v.tau0, operator="reg", les=True, flags=grid.flags,
@@ -495,7 +521,8 @@ def main():
                    "l2": "inputs larger than L2 (2.5 GB populations)"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                     "kernel": "aa_step_fast + aa_step_seam (plain cells, two per thread)",
+                     "kernel": "aa_step_pairs (even steps) + aa_step_fast + aa_step_seam (odd steps): plain cells, "
+                               "two per thread",
                      "bytes_per_cell": BYTES["f16"], "cells_per_step": n_plain,
                      "ms_per_step": round(plain_s * 1e3, 4),
                      "traffic": traffic.get("bytes_per_step") if traffic else None,

@@ -172,6 +172,7 @@ struct pw_domain {
   uint64_t first_fluid = ~0ull;
   cudaStream_t stream = nullptr;
   cudaEvent_t force_event = nullptr;
+  pwfast::SideStream side;        // edge and seam kernels of split steps run here, beside the plain kernel
   uint64_t steps = 0;
   int force_state = FORCE_IDLE;
   uint64_t force_step = 0;
@@ -265,7 +266,7 @@ void enqueue_step(pw_domain *d, uint64_t step, float u_in, int write_macro) {
                                         d->stream);
   else if (d->split)
     pwfast::launch_step_split(p, d->desc.storage, d->desc.op, d->desc.les, odd, d->plain_grid, d->edges,
-                              d->edge_count, d->stream);
+                              d->edge_count, d->stream, nullptr, &d->side);
   else
     pwfast::launch_step(p, d->desc.storage, d->desc.op, d->desc.les, odd, d->grid, d->stream);
 }
@@ -320,6 +321,13 @@ int launch_init(pw_domain *d) {
   }
   PW_TRY(cudaGetLastError());
   return PW_OK;
+}
+
+void destroy_side(pw_domain *d) {
+  if (d->side.stream) cudaStreamDestroy(d->side.stream);
+  if (d->side.fork) cudaEventDestroy(d->side.fork);
+  if (d->side.join) cudaEventDestroy(d->side.join);
+  d->side = pwfast::SideStream();
 }
 
 int ensure_scratch(pw_domain *d) {
@@ -478,6 +486,13 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
   Allocs a;
   cudaError_t e = cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&d->force_event, cudaEventDisableTiming);
+  // the side stream takes the highest priority, so the edge kernel's few blocks
+  // are dispatched ahead of the plain kernel's grid instead of after it
+  int lo_prio = 0, hi_prio = 0;
+  if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&d->side.stream, cudaStreamNonBlocking, hi_prio);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&d->side.fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&d->side.join, cudaEventDisableTiming);
   // The fast step's two-cell kernel reads (and discards) elements up to
   // nx * ny + nx + 64 past the 19 direction planes.
   if (e == cudaSuccess)
@@ -503,6 +518,7 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
     if (d->force_host) cudaFreeHost(d->force_host);
     if (d->status_host) cudaFreeHost(d->status_host);
     if (d->force_event) cudaEventDestroy(d->force_event);
+    destroy_side(d);
     if (d->stream) cudaStreamDestroy(d->stream);
     delete d;
     return rc;
@@ -541,6 +557,7 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
     cudaFreeHost(d->force_host);
     cudaFreeHost(d->status_host);
     cudaEventDestroy(d->force_event);
+    destroy_side(d);
     cudaStreamDestroy(d->stream);
     delete d;
     return rc;
@@ -562,6 +579,7 @@ void pw_domain_destroy(pw_domain *d) {
   cudaFree(d->qoff); cudaFree(d->qfrac); cudaFree(d->hist);
   cudaFreeHost(d->force_host); cudaFreeHost(d->status_host);
   cudaEventDestroy(d->force_event);
+  destroy_side(d);
   cudaStreamDestroy(d->stream);
   cudaGetLastError();
   delete d;

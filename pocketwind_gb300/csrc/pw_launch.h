@@ -37,12 +37,23 @@
 
 PW_DECLARE_LAUNCHERS(pwfast)
 namespace pwfast {
+// A second stream for the edge and seam-row kernels of a split step, forked
+// from and joined back to the step's stream by the two events.
+struct SideStream {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
 // The fast build's split step: plain cells over plain_grid (the cell grid),
-// then the listed edge cells, whose blocks own the force partials.  With ev
-// (6 events) it records around the plain kernel (0, 1), the seam-row kernel
-// (2, 3) and the edge kernel (4, 5).
+// the seam rows (odd steps) and the listed edge cells, whose blocks own the
+// force partials.  The three kernels update disjoint cells, and in the in-place
+// pattern no cell reads a slot that another writes within a step, so with side
+// the seam and edge kernels run on side.stream concurrently with the plain
+// kernel and join before the step ends.  With ev (6 events, no side stream) it
+// records around the plain kernel (0, 1), the seam-row kernel (2, 3) and the
+// edge kernel (4, 5).
 void launch_step_split(const pw::StepParams &p, int storage, int op, int les, bool odd, dim3 plain_grid,
-                       const uint32_t *list, uint32_t count, cudaStream_t s, const cudaEvent_t *ev = nullptr);
+                       const uint32_t *list, uint32_t count, cudaStream_t s, const cudaEvent_t *ev = nullptr,
+                       const SideStream *side = nullptr);
 void launch_refresh_edges(const pw::StepParams &p, int odd_layout, int storage, const uint32_t *list,
                           uint32_t count, cudaStream_t s);
 }

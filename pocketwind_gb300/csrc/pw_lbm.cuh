@@ -1494,8 +1494,24 @@ static inline void mark(const cudaEvent_t *ev, int k, cudaStream_t s) {
 }
 template <int ST, int OP, bool LES>
 static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *list, uint32_t count, cudaStream_t s,
-                        const cudaEvent_t *ev) {
-  if (g.x && g.y && g.z) {
+                        const cudaEvent_t *ev, const SideStream *side) {
+  const bool plain = g.x && g.y && g.z;
+  // the seam and edge kernels: on the side stream when there is one
+  cudaStream_t t = side ? side->stream : s;
+  if (side) {
+    cudaEventRecord(side->fork, s);
+    cudaStreamWaitEvent(t, side->fork, 0);
+  }
+  if (side) {
+    // launched first so their few blocks start before the plain grid fills the GPU
+    if (plain && odd) aa_step_seam<ST, OP, LES><<<dim3(g.x, seam_rows(p.ny, p.nz)), BX, 0, t>>>(p);
+    if (count) {
+      unsigned blocks = (count + NTHREADS - 1) / NTHREADS;
+      if (odd) aa_step_edges<ST, OP, LES, true><<<blocks, NTHREADS, 0, t>>>(p, list, count);
+      else aa_step_edges<ST, OP, LES, false><<<blocks, NTHREADS, 0, t>>>(p, list, count);
+    }
+  }
+  if (plain) {
     const unsigned runs = (p.nx + 2 * BX - 1) / (2 * BX);  // 64-cell runs per row
     // even steps of 16-bit storage with whole 32-bit pairs in a row: the pair kernel
     const bool pairs = ST != STORE_F32 && (p.nx & 1u) == 0u;
@@ -1505,7 +1521,7 @@ static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *l
       if (inner.y && inner.z) aa_step_fast<ST, OP, LES, true><<<inner, dim3(BX, BY), 0, s>>>(p);
       mark(ev, 1, s);
       mark(ev, 2, s);
-      aa_step_seam<ST, OP, LES><<<dim3(g.x, seam_rows(p.ny, p.nz)), BX, 0, s>>>(p);
+      if (!side) aa_step_seam<ST, OP, LES><<<dim3(g.x, seam_rows(p.ny, p.nz)), BX, 0, s>>>(p);
       mark(ev, 3, s);
     } else {
       mark(ev, 0, s);
@@ -1521,6 +1537,11 @@ static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *l
       mark(ev, 3, s);
     }
   }
+  if (side) {
+    cudaEventRecord(side->join, t);
+    cudaStreamWaitEvent(s, side->join, 0);
+    return;
+  }
   mark(ev, 4, s);
   if (count) {
     unsigned blocks = (count + NTHREADS - 1) / NTHREADS;
@@ -1531,21 +1552,23 @@ static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *l
 }
 template <int ST>
 static void step_split2(const StepParams &p, int op, int les, bool odd, dim3 g, const uint32_t *list, uint32_t count,
-                        cudaStream_t s, const cudaEvent_t *ev) {
+                        cudaStream_t s, const cudaEvent_t *ev, const SideStream *side) {
   if (op == OP_REG) {
-    if (les) step_split3<ST, OP_REG, true>(p, odd, g, list, count, s, ev);
-    else step_split3<ST, OP_REG, false>(p, odd, g, list, count, s, ev);
+    if (les) step_split3<ST, OP_REG, true>(p, odd, g, list, count, s, ev, side);
+    else step_split3<ST, OP_REG, false>(p, odd, g, list, count, s, ev, side);
   } else {
-    if (les) step_split3<ST, OP_TRT, true>(p, odd, g, list, count, s, ev);
-    else step_split3<ST, OP_TRT, false>(p, odd, g, list, count, s, ev);
+    if (les) step_split3<ST, OP_TRT, true>(p, odd, g, list, count, s, ev, side);
+    else step_split3<ST, OP_TRT, false>(p, odd, g, list, count, s, ev, side);
   }
 }
 void launch_step_split(const StepParams &p, int storage, int op, int les, bool odd, dim3 plain_grid,
-                       const uint32_t *list, uint32_t count, cudaStream_t s, const cudaEvent_t *ev) {
+                       const uint32_t *list, uint32_t count, cudaStream_t s, const cudaEvent_t *ev,
+                       const SideStream *side) {
+  if (ev) side = nullptr;  // per-kernel timing runs the kernels one after another
   switch (storage) {
-    case STORE_F16: step_split2<STORE_F16>(p, op, les, odd, plain_grid, list, count, s, ev); break;
-    case STORE_BF16: step_split2<STORE_BF16>(p, op, les, odd, plain_grid, list, count, s, ev); break;
-    default: step_split2<STORE_F32>(p, op, les, odd, plain_grid, list, count, s, ev); break;
+    case STORE_F16: step_split2<STORE_F16>(p, op, les, odd, plain_grid, list, count, s, ev, side); break;
+    case STORE_BF16: step_split2<STORE_BF16>(p, op, les, odd, plain_grid, list, count, s, ev, side); break;
+    default: step_split2<STORE_F32>(p, op, les, odd, plain_grid, list, count, s, ev, side); break;
   }
 }
 #endif
