@@ -4,14 +4,19 @@
 // reference, which runs one solver at a time (src/app/solver-slot.ts).
 //
 // Work items (per step parity):
-//   plain  R rows x 64 cells of one member (plain_thread: two cells per thread;
+//   plain  R rows x 64 cells of one member (two cells per thread: the 32-bit
+//          cell-pair kernel on even steps of 16-bit storage, x / x + 32 else;
 //          even steps every row, odd steps the rows off the y/z seams);
 //   seam   4 seam rows x 32 cells (odd steps; seam_thread);
 //   edge   128 listed cells (edge_block), whose force partial goes to the
 //          member's slot of that block, exactly as its own edge kernel does.
-// A block loads its item's member parameters into shared memory and runs the
-// same device code as the member's own kernels, so a member stepped in a batch
-// follows the same arithmetic as one stepped alone.
+// A step is two persistent launches, as a single domain's step is: the plain
+// items, and the seam and edge items on a high-priority side stream beside
+// them (disjoint cells, so they may run together), each kernel with only its
+// own code path and registers.  A block loads its item's member parameters
+// into shared memory and runs the same device code as the member's own
+// kernels, so a member stepped in a batch follows the same arithmetic as one
+// stepped alone.
 #define PW_NS pwbatch
 #define PW_STRICT 0
 #include <algorithm>
@@ -47,8 +52,13 @@ __device__ __forceinline__ uint32_t seg_of(const BatchSeg *segs, uint32_t nsegs,
   return lo;
 }
 
-template <int ST, int OP, bool LES, bool ODD>
-__global__ void __launch_bounds__(kBatchThreads) batch_step(const StepParams *params, const BatchSeg *segs,
+// PLAIN: the plain items (PAIRS: through the 32-bit cell-pair kernel, which
+// needs an even step, 16-bit storage and every member's nx even); otherwise
+// the seam and edge items.
+// The plain kernels are held to 85 registers (6 blocks per SM): the member's
+// offset tables sit in shared memory and are reloaded rather than kept live.
+template <int ST, int OP, bool LES, bool ODD, bool PLAIN, bool PAIRS>
+__global__ void __launch_bounds__(kBatchThreads, PLAIN ? 6 : 1) batch_step(const StepParams *params, const BatchSeg *segs,
                                                              uint32_t nsegs, uint32_t total,
                                                              const uint32_t *const *lists, const uint32_t *counts,
                                                              uint32_t rows) {
@@ -66,17 +76,20 @@ __global__ void __launch_bounds__(kBatchThreads) batch_step(const StepParams *pa
       for (uint32_t i = tid; i < sizeof(StepParams) / 4; i += kBatchThreads) dst[i] = src[i];
     }
     __syncthreads();
-    if (kind == 0) {
+    if (PLAIN) {
       const uint32_t off = ODD ? 1u : 0u;
       const uint32_t runs = (sp.nx + 63u) / 64u;
       const uint32_t ny_rows = sp.ny - 2u * off;
       const uint32_t yblocks = (ny_rows + rows - 1u) / rows;
       const uint32_t run = local % runs, t = local / runs;
       const uint32_t yb = t % yblocks, zb = t / yblocks;
-      const uint32_t x = run * 64u + (tid & 31u);
       for (uint32_t r = tid >> 5; r < rows; r += kBatchThreads / 32) {
         const uint32_t yr = yb * rows + r;
-        if (yr < ny_rows) pwbatch::plain_thread<ST, OP, LES, ODD>(sp, x, yr + off, zb + off);
+        if (yr >= ny_rows) continue;
+        if constexpr (PAIRS && !ODD && ST != pw::STORE_F32)
+          pwbatch::pair_thread<ST, OP, LES>(sp, run * 64u + 2u * (tid & 31u), yr, zb);
+        else
+          pwbatch::plain_thread<ST, OP, LES, ODD>(sp, run * 64u + (tid & 31u), yr + off, zb + off);
       }
     } else if (kind == 1) {
       const uint32_t runs = (sp.nx + 31u) / 32u;
@@ -90,22 +103,32 @@ __global__ void __launch_bounds__(kBatchThreads) batch_step(const StepParams *pa
 }
 
 template <int ST, int OP, bool LES>
-void launch3(bool odd, unsigned blocks, cudaStream_t s, const StepParams *params, const BatchSeg *segs,
-             uint32_t nsegs, uint32_t total, const uint32_t *const *lists, const uint32_t *counts, uint32_t rows) {
-  if (odd) batch_step<ST, OP, LES, true><<<blocks, kBatchThreads, 0, s>>>(params, segs, nsegs, total, lists, counts, rows);
-  else batch_step<ST, OP, LES, false><<<blocks, kBatchThreads, 0, s>>>(params, segs, nsegs, total, lists, counts, rows);
+void launch3(bool odd, bool plain, bool pairs, unsigned blocks, cudaStream_t s, const StepParams *params,
+             const BatchSeg *segs, uint32_t nsegs, uint32_t total, const uint32_t *const *lists,
+             const uint32_t *counts, uint32_t rows) {
+#define PW_BATCH_LAUNCH(O, P, Q) \
+  batch_step<ST, OP, LES, O, P, Q><<<blocks, kBatchThreads, 0, s>>>(params, segs, nsegs, total, lists, counts, rows)
+  if (plain) {
+    if (odd) PW_BATCH_LAUNCH(true, true, false);
+    else if (pairs && ST != pw::STORE_F32) PW_BATCH_LAUNCH(false, true, true);
+    else PW_BATCH_LAUNCH(false, true, false);
+  } else {
+    if (odd) PW_BATCH_LAUNCH(true, false, false);
+    else PW_BATCH_LAUNCH(false, false, false);
+  }
+#undef PW_BATCH_LAUNCH
 }
 
 template <int ST>
-void launch2(int op, int les, bool odd, unsigned blocks, cudaStream_t s, const StepParams *params,
-             const BatchSeg *segs, uint32_t nsegs, uint32_t total, const uint32_t *const *lists,
-             const uint32_t *counts, uint32_t rows) {
+void launch2(int op, int les, bool odd, bool plain, bool pairs, unsigned blocks, cudaStream_t s,
+             const StepParams *params, const BatchSeg *segs, uint32_t nsegs, uint32_t total,
+             const uint32_t *const *lists, const uint32_t *counts, uint32_t rows) {
   if (op == pw::OP_REG) {
-    if (les) launch3<ST, pw::OP_REG, true>(odd, blocks, s, params, segs, nsegs, total, lists, counts, rows);
-    else launch3<ST, pw::OP_REG, false>(odd, blocks, s, params, segs, nsegs, total, lists, counts, rows);
+    if (les) launch3<ST, pw::OP_REG, true>(odd, plain, pairs, blocks, s, params, segs, nsegs, total, lists, counts, rows);
+    else launch3<ST, pw::OP_REG, false>(odd, plain, pairs, blocks, s, params, segs, nsegs, total, lists, counts, rows);
   } else {
-    if (les) launch3<ST, pw::OP_TRT, true>(odd, blocks, s, params, segs, nsegs, total, lists, counts, rows);
-    else launch3<ST, pw::OP_TRT, false>(odd, blocks, s, params, segs, nsegs, total, lists, counts, rows);
+    if (les) launch3<ST, pw::OP_TRT, true>(odd, plain, pairs, blocks, s, params, segs, nsegs, total, lists, counts, rows);
+    else launch3<ST, pw::OP_TRT, false>(odd, plain, pairs, blocks, s, params, segs, nsegs, total, lists, counts, rows);
   }
 }
 
@@ -117,10 +140,15 @@ struct pw_batch {
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
   std::vector<cudaEvent_t> member_ready;
-  // [parity][write_macro] member parameter arrays; [parity] work segments
+  // [parity][write_macro] member parameter arrays; [parity][plain items, seam and
+  // edge items] work segments
   StepParams *params[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-  BatchSeg *segs[2] = {nullptr, nullptr};
-  uint32_t nsegs[2] = {0, 0}, total[2] = {0, 0};
+  BatchSeg *segs[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  uint32_t nsegs[2][2] = {{0, 0}, {0, 0}}, total[2][2] = {{0, 0}, {0, 0}};
+  cudaStream_t side = nullptr;    // the seam and edge items, beside the plain items
+  cudaEvent_t fork = nullptr, join = nullptr;
+  unsigned sms = 1;               // multiprocessors of the device
+  bool pairs = false;             // every member's nx is even: even steps use the cell-pair kernel
   const uint32_t **lists = nullptr;
   uint32_t *counts = nullptr;
   uint32_t rows = 4;       // plain rows per work item
@@ -139,8 +167,8 @@ void drop_graphs(pw_batch *b) {
 // Work segments of both parities for the current rows-per-item.
 int build_segments(pw_batch *b) {
   for (int par = 0; par < 2; par++) {
-    std::vector<BatchSeg> segs;
-    uint32_t first = 0;
+    std::vector<BatchSeg> segs[2];
+    uint32_t first[2] = {0, 0};
     for (uint32_t m = 0; m < b->members.size(); m++) {
       const MemberView v = member_view(b->members[m]);
       const uint32_t off = par ? 1u : 0u;
@@ -152,17 +180,21 @@ int build_segments(pw_batch *b) {
       const uint32_t kinds[3] = {plain, seam, edge};
       for (uint32_t k = 0; k < 3; k++) {
         if (!kinds[k]) continue;
-        segs.push_back(BatchSeg{first, m, k, kinds[k]});
-        first += kinds[k];
+        const int list = k == 0 ? 0 : 1;
+        segs[list].push_back(BatchSeg{first[list], m, k, kinds[k]});
+        first[list] += kinds[k];
       }
     }
-    if (segs.empty()) segs.push_back(BatchSeg{0, 0, 0, 0});
-    cudaFree(b->segs[par]);
-    b->segs[par] = nullptr;
-    PW_TRY(cudaMalloc(&b->segs[par], segs.size() * sizeof(BatchSeg)));
-    PW_TRY(cudaMemcpy(b->segs[par], segs.data(), segs.size() * sizeof(BatchSeg), cudaMemcpyHostToDevice));
-    b->nsegs[par] = (uint32_t)segs.size();
-    b->total[par] = first;
+    for (int list = 0; list < 2; list++) {
+      if (segs[list].empty()) segs[list].push_back(BatchSeg{0, 0, (uint32_t)list, 0});
+      cudaFree(b->segs[par][list]);
+      b->segs[par][list] = nullptr;
+      PW_TRY(cudaMalloc(&b->segs[par][list], segs[list].size() * sizeof(BatchSeg)));
+      PW_TRY(cudaMemcpy(b->segs[par][list], segs[list].data(), segs[list].size() * sizeof(BatchSeg),
+                        cudaMemcpyHostToDevice));
+      b->nsegs[par][list] = (uint32_t)segs[list].size();
+      b->total[par][list] = first[list];
+    }
   }
   return PW_OK;
 }
@@ -182,24 +214,44 @@ int upload_params(pw_batch *b) {
   return PW_OK;
 }
 
+void launch_items(pw_batch *b, bool odd, int macro, bool plain, unsigned blocks, cudaStream_t s) {
+  const int par = odd ? 1 : 0, list = plain ? 0 : 1;
+  const StepParams *params = b->params[par][macro];
+  const BatchSeg *segs = b->segs[par][list];
+  const uint32_t nsegs = b->nsegs[par][list], total = b->total[par][list];
+  switch (b->storage) {
+    case pw::STORE_F16:
+      launch2<pw::STORE_F16>(b->op, b->les, odd, plain, b->pairs, blocks, s, params, segs, nsegs, total, b->lists,
+                             b->counts, b->rows);
+      break;
+    case pw::STORE_BF16:
+      launch2<pw::STORE_BF16>(b->op, b->les, odd, plain, b->pairs, blocks, s, params, segs, nsegs, total, b->lists,
+                              b->counts, b->rows);
+      break;
+    default:
+      launch2<pw::STORE_F32>(b->op, b->les, odd, plain, b->pairs, blocks, s, params, segs, nsegs, total, b->lists,
+                             b->counts, b->rows);
+      break;
+  }
+}
+
 void enqueue(pw_batch *b, bool odd, int macro) {
   const int par = odd ? 1 : 0;
   if (macro)
     for (pw_domain *d : b->members) cudaMemsetAsync(member_view(d).status, 0, 4, b->stream);
-  const unsigned blocks = std::max(1u, std::min<unsigned>(b->blocks, std::max(1u, b->total[par])));
-  switch (b->storage) {
-    case pw::STORE_F16:
-      launch2<pw::STORE_F16>(b->op, b->les, odd, blocks, b->stream, b->params[par][macro], b->segs[par],
-                             b->nsegs[par], b->total[par], b->lists, b->counts, b->rows);
-      break;
-    case pw::STORE_BF16:
-      launch2<pw::STORE_BF16>(b->op, b->les, odd, blocks, b->stream, b->params[par][macro], b->segs[par],
-                              b->nsegs[par], b->total[par], b->lists, b->counts, b->rows);
-      break;
-    default:
-      launch2<pw::STORE_F32>(b->op, b->les, odd, blocks, b->stream, b->params[par][macro], b->segs[par],
-                             b->nsegs[par], b->total[par], b->lists, b->counts, b->rows);
-      break;
+  const uint32_t rest = b->total[par][1];
+  if (rest) {
+    // seam and edge items on the side stream, forked from and joined back to the batch stream
+    cudaEventRecord(b->fork, b->stream);
+    cudaStreamWaitEvent(b->side, b->fork, 0);
+    const unsigned rblocks = std::max(1u, std::min<unsigned>(rest, b->sms * 8u));
+    launch_items(b, odd, macro, false, rblocks, b->side);
+  }
+  const unsigned blocks = std::max(1u, std::min<unsigned>(b->blocks, std::max(1u, b->total[par][0])));
+  if (b->total[par][0]) launch_items(b, odd, macro, true, blocks, b->stream);
+  if (rest) {
+    cudaEventRecord(b->join, b->side);
+    cudaStreamWaitEvent(b->stream, b->join, 0);
   }
 }
 
@@ -295,14 +347,22 @@ int pw_batch_create(pw_domain *const *members, uint32_t count, pw_batch **out) {
   }
   pw_batch *b = new pw_batch();
   b->members.assign(members, members + count);
+  b->pairs = true;
+  for (uint32_t m = 0; m < count; m++) b->pairs = b->pairs && (member_view(members[m]).nx & 1u) == 0u;
   b->storage = first.storage; b->op = first.op; b->les = first.les;
   b->steps = first.steps;
-  b->blocks = (unsigned)max_blocks() * 4u;
+  b->sms = (unsigned)max_blocks();
+  b->blocks = b->sms * 4u;
   auto fail = [&](int rc) {
     pw_batch_destroy(b);
     return rc;
   };
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  int lo_prio = 0, hi_prio = 0;
+  if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&b->side, cudaStreamNonBlocking, hi_prio);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
   b->member_ready.assign(count, nullptr);
   for (uint32_t m = 0; m < count && e == cudaSuccess; m++)
@@ -336,8 +396,11 @@ void pw_batch_destroy(pw_batch *b) {
   drop_graphs(b);
   for (int par = 0; par < 2; par++) {
     for (int macro = 0; macro < 2; macro++) cudaFree(b->params[par][macro]);
-    cudaFree(b->segs[par]);
+    for (int list = 0; list < 2; list++) cudaFree(b->segs[par][list]);
   }
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->join) cudaEventDestroy(b->join);
+  if (b->side) cudaStreamDestroy(b->side);
   cudaFree(b->lists);
   cudaFree(b->counts);
   for (cudaEvent_t ev : b->member_ready)

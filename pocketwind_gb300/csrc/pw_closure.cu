@@ -56,30 +56,33 @@ __device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], const 
 // the biases in the accumulator layout (columns 2t, 2t+1 of each 8-wide tile).
 __global__ void build_fragments(const float *w, uint32_t *frag) {
   const uint32_t lane = threadIdx.x, g = lane >> 2, t = lane & 3;
-  uint32_t *o = frag + lane * kFragWords;
+  // word k of lane l at frag[32 k + l]: a warp loads each word as one 128-byte line
+  auto put = [&](uint32_t k, uint32_t v) { frag[32 * k + lane] = v; };
   auto w1 = [&](uint32_t n, uint32_t k) { return k < (uint32_t)kIn ? w[kW1 + n * kIn + k] : 0.0f; };
   auto w2 = [&](uint32_t n, uint32_t k) { return w[kW2 + n * kHidden + k]; };
   auto w3 = [&](uint32_t k) { return g == 0 ? w[kW3 + k] : 0.0f; };
   for (uint32_t j = 0; j < 4; j++) {
     const uint32_t n = 8 * j + g;
-    o[2 * j] = pack_bf16(w1(n, 2 * t), w1(n, 2 * t + 1));
-    o[2 * j + 1] = pack_bf16(w1(n, 2 * t + 8), w1(n, 2 * t + 9));
+    put(2 * j, pack_bf16(w1(n, 2 * t), w1(n, 2 * t + 1)));
+    put(2 * j + 1, pack_bf16(w1(n, 2 * t + 8), w1(n, 2 * t + 9)));
     for (uint32_t kt = 0; kt < 2; kt++) {
       const uint32_t kb = 16 * kt;
-      o[8 + (2 * j + kt) * 2] = pack_bf16(w2(n, kb + 2 * t), w2(n, kb + 2 * t + 1));
-      o[8 + (2 * j + kt) * 2 + 1] = pack_bf16(w2(n, kb + 2 * t + 8), w2(n, kb + 2 * t + 9));
+      put(8 + (2 * j + kt) * 2, pack_bf16(w2(n, kb + 2 * t), w2(n, kb + 2 * t + 1)));
+      put(8 + (2 * j + kt) * 2 + 1, pack_bf16(w2(n, kb + 2 * t + 8), w2(n, kb + 2 * t + 9)));
     }
-    o[28 + 2 * j] = __float_as_uint(w[kB1 + 8 * j + 2 * t]);
-    o[29 + 2 * j] = __float_as_uint(w[kB1 + 8 * j + 2 * t + 1]);
-    o[36 + 2 * j] = __float_as_uint(w[kB2 + 8 * j + 2 * t]);
-    o[37 + 2 * j] = __float_as_uint(w[kB2 + 8 * j + 2 * t + 1]);
+    put(28 + 2 * j, __float_as_uint(w[kB1 + 8 * j + 2 * t]));
+    put(29 + 2 * j, __float_as_uint(w[kB1 + 8 * j + 2 * t + 1]));
+    put(36 + 2 * j, __float_as_uint(w[kB2 + 8 * j + 2 * t]));
+    put(37 + 2 * j, __float_as_uint(w[kB2 + 8 * j + 2 * t + 1]));
   }
   for (uint32_t kt = 0; kt < 2; kt++) {
-    o[24 + 2 * kt] = pack_bf16(w3(16 * kt + 2 * t), w3(16 * kt + 2 * t + 1));
-    o[25 + 2 * kt] = pack_bf16(w3(16 * kt + 2 * t + 8), w3(16 * kt + 2 * t + 9));
+    put(24 + 2 * kt, pack_bf16(w3(16 * kt + 2 * t), w3(16 * kt + 2 * t + 1)));
+    put(25 + 2 * kt, pack_bf16(w3(16 * kt + 2 * t + 8), w3(16 * kt + 2 * t + 9)));
   }
-  o[44] = __float_as_uint(w[kB3]);
-  o[45] = o[46] = o[47] = 0u;
+  put(44, __float_as_uint(w[kB3]));
+  put(45, 0u);
+  put(46, 0u);
+  put(47, 0u);
 }
 
 // This lane's operand fragments and biases, held in registers across cells.
@@ -89,20 +92,20 @@ struct Frag {
 };
 
 __device__ __forceinline__ Frag load_frag(const uint32_t *frag) {
-  const uint32_t *fr = frag + (threadIdx.x & 31u) * kFragWords;
+  const uint32_t *fr = frag + (threadIdx.x & 31u);
   Frag f;
 #pragma unroll
-  for (int k = 0; k < 8; k++) f.w1[k] = __ldg(&fr[k]);
+  for (int k = 0; k < 8; k++) f.w1[k] = __ldg(&fr[32 * k]);
 #pragma unroll
-  for (int k = 0; k < 16; k++) f.w2[k] = __ldg(&fr[8 + k]);
+  for (int k = 0; k < 16; k++) f.w2[k] = __ldg(&fr[32 * (8 + k)]);
 #pragma unroll
-  for (int k = 0; k < 4; k++) f.w3[k] = __ldg(&fr[24 + k]);
+  for (int k = 0; k < 4; k++) f.w3[k] = __ldg(&fr[32 * (24 + k)]);
 #pragma unroll
   for (int k = 0; k < 8; k++) {
-    f.b1[k] = __uint_as_float(__ldg(&fr[28 + k]));
-    f.b2[k] = __uint_as_float(__ldg(&fr[36 + k]));
+    f.b1[k] = __uint_as_float(__ldg(&fr[32 * (28 + k)]));
+    f.b2[k] = __uint_as_float(__ldg(&fr[32 * (36 + k)]));
   }
-  f.b3 = __uint_as_float(__ldg(&fr[44]));
+  f.b3 = __uint_as_float(__ldg(&fr[32 * 44]));
   return f;
 }
 
