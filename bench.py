@@ -27,8 +27,9 @@ cpu_baseline: the binary64 restatement of the reference's CpuSolver (the
           host cores, over a bounded number of full-domain steps.
 accuracy: drag and field errors against that binary64 restatement: the sphere
           at Re 100 (96x48x48, FP32) and the 128x64x64 vehicle in each storage.
-batched_tunnels: 64 seeded tunnels of uneven size and Re, FP16 TRT, one
-          persistent launch per step from captured graphs, autotuned shape;
+batched_tunnels: 64 seeded tunnels of uneven size and Re, FP16 TRT, two
+          concurrent persistent launches per step from captured graphs,
+          autotuned shape;
           aggregate MLUPS and drag error against each tunnel alone in FP32.
 
 --impl reference runs only that CPU path and prints its own line.
@@ -271,9 +272,9 @@ def accuracy_leg(steps, threads):
 
 def batch_leg(steps, sample_steps=200, count=64, peak=None):
     """64 independent tunnels (sizes, bodies and Re from splitmix64 seed 1), FP16
-    storage, TRT, stepped as one batch: one persistent launch per step over all
-    members, replayed from captured 50-step graphs, launch shape from the
-    autotuner.  Aggregate MLUPS over `steps` steps, then each member's drag over
+    storage, TRT, stepped as one batch: per step one persistent launch over all
+    members' plain cells and one over their seam and edge cells beside it,
+    replayed from captured 50-step graphs, launch shape from the autotuner.  Aggregate MLUPS over `steps` steps, then each member's drag over
     the last `sample_steps` steps against the same tunnel run alone in FP32."""
     import numpy as np
     from pocketwind_gb300 import cases, geometry, solver
@@ -318,7 +319,7 @@ def batch_leg(steps, sample_steps=200, count=64, peak=None):
     mlups = cells * steps / (ms * 1e3)
     out = {"domains": count, "cells": cells, "steps": steps, "storage": "f16", "operator": "trt",
            "ms_per_step": round(ms / steps, 4), "mlups": round(mlups, 1),
-           "launches_per_step": 1, "graph_chunk_steps": 50,
+           "launches_per_step": 2, "graph_chunk_steps": 50,
            "tuning": {"blocks": tuning.blocks, "rows_per_item": tuning.rows_per_item,
                       "candidates": tuning.candidates},
            "drag_rel_err_vs_solo_f32": {"median": float(np.median(err)), "p90": float(np.percentile(err, 90)),

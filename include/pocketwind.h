@@ -237,7 +237,8 @@ PW_API int pw_checkpoint_load(pw_domain *dom, const void *in, size_t size);
    the reference runs one solver at a time, src/app/solver-slot.ts) ----
    Members are domains of the fast build's one-cell-per-thread path sharing
    storage, operator and LES, with equal step counts and no ramp in progress.
-   Each batch step is one persistent launch over all members' work, replayed
+   Each batch step is two persistent launches, one over all members' plain
+   cells and one over their seam and edge cells running beside it, replayed
    from captured CUDA graphs; members keep their own force, macro and readout
    calls, which wait for the batch's queued steps.  A member must not be
    stepped on its own while it belongs to a batch. */
