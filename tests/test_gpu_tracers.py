@@ -103,3 +103,29 @@ def test_streaks_match_restatement():
     assert np.array_equal(got[:, :3], ref[:, :3])
     assert np.allclose(got[:, 3], ref[:, 3], rtol=1e-4, atol=0)
     assert (got[:, 3] > 0).sum() > 1000
+
+
+def test_plate_smoke_with_dye_ports_from_geometry():
+    """The plate's ports placed by dye_ports (plate-layout.ts:164-225) on the
+    voxelized vehicle's centre plane, the rake from rake_span: the kernel
+    matches the restatement and the port threads carry live smoke."""
+    from pocketwind_gb300 import plate_layout as PL
+    from pocketwind_gb300.tracers import PlateSmoke
+    s, grid = _flow_case()
+    flags = grid.flags.copy()
+    macros = s.macros().reshape(-1)
+    low, high = PL.rake_span(44.0, 64)
+    ports = PL.dye_ports(flags, (128, 64, 64), 32, (low, high)).reshape(-1, 2)
+    assert (ports[:, 0] >= 0).sum() >= 4
+    plate = PlateSmoke(s, 32, PL.RAKE_THREADS, 64, ports)
+    ref = np.zeros((PL.THREADS * 64, 4), np.float32)
+    rake = (float(PL.RAKE_X), low, high, 8.0)
+    for frame in range(30):
+        release, releasing = frame // 2, frame % 2 == 0
+        plate.advance(release, releasing, rake)
+        ref = O.plate_smoke(ref, PL.THREADS, 64, release, releasing, rake, (128, 64, 64), 32, macros, flags, ports)
+    got = plate.read()
+    assert np.array_equal(got[:, :3], ref.reshape(-1, 4)[:, :3])
+    port_rows = got.reshape(PL.THREADS, 64, 4)[PL.RAKE_THREADS:]
+    live = [(port_rows[k, :, 3] > 0).any() for k in range(PL.PORTS) if ports[k, 0] >= 0]
+    assert all(live)
