@@ -129,3 +129,28 @@ def test_plate_smoke_with_dye_ports_from_geometry():
     port_rows = got.reshape(PL.THREADS, 64, 4)[PL.RAKE_THREADS:]
     live = [(port_rows[k, :, 3] > 0).any() for k in range(PL.PORTS) if ports[k, 0] >= 0]
     assert all(live)
+
+
+def test_particles_seeded_from_geometry_stay_valid():
+    """particle_seeds (particle-layout.ts:66-112) on the voxelized vehicle feeds
+    the particle kernel; after advection every particle sits on a valid fluid
+    node by the reseed rule the kernel applies."""
+    from pocketwind_gb300 import meshes, particle_layout as PL
+    from pocketwind_gb300.tracers import Particles
+    s, grid = _flow_case()
+    layout = (128, 64, 64)
+    body = meshes.vehicle_case_mesh(128, 64)
+    pts = body.positions.reshape(-1, 3)
+    data, region, fallback = PL.particle_seeds(grid.flags, layout, pts.min(axis=0), pts.max(axis=0), 4096, 7)
+    p = Particles(s, data, 7, region, fallback)
+    for _ in range(20):
+        p.update(8.0)
+    rec = p.read().reshape(-1, 8)
+    flags = grid.flags
+    bad = 0
+    for r in rec[::17]:
+        x, y, z, age = (float(v) for v in r[:4])
+        n = int(round(x)) + 128 * (int(round(y)) + 64 * int(round(z)))
+        flag = int(flags[n]) if 0 <= n < flags.size else 1
+        bad += PL.particle_needs_reseed((x, y, z), age, layout, flag)
+    assert bad == 0
