@@ -5,7 +5,7 @@
 //
 // Work items (per step parity):
 //   plain  R rows x 64 cells of one member (two cells per thread: the 32-bit
-//          cell-pair kernel on even steps of 16-bit storage, x / x + 32 else;
+//          cell-pair kernel for 16-bit storage, x / x + 32 else;
 //          even steps every row, odd steps the rows off the y/z seams);
 //   seam   4 seam rows x 32 cells (odd steps; seam_thread);
 //   edge   128 listed cells (edge_block), whose force partial goes to the
@@ -53,7 +53,7 @@ __device__ __forceinline__ uint32_t seg_of(const BatchSeg *segs, uint32_t nsegs,
 }
 
 // PLAIN: the plain items (PAIRS: through the 32-bit cell-pair kernel, which
-// needs an even step, 16-bit storage and every member's nx even); otherwise
+// needs 16-bit storage and every member's nx even); otherwise
 // the seam and edge items.
 // The plain kernels are held to 85 registers (6 blocks per SM): the member's
 // offset tables sit in shared memory and are reloaded rather than kept live.
@@ -86,8 +86,8 @@ __global__ void __launch_bounds__(kBatchThreads, PLAIN ? 6 : 1) batch_step(const
       for (uint32_t r = tid >> 5; r < rows; r += kBatchThreads / 32) {
         const uint32_t yr = yb * rows + r;
         if (yr >= ny_rows) continue;
-        if constexpr (PAIRS && !ODD && ST != pw::STORE_F32)
-          pwbatch::pair_thread<ST, OP, LES>(sp, run * 64u + 2u * (tid & 31u), yr, zb);
+        if constexpr (PAIRS && ST != pw::STORE_F32)
+          pwbatch::pair_thread<ST, OP, LES, ODD>(sp, run * 64u + 2u * (tid & 31u), yr + off, zb + off);
         else
           pwbatch::plain_thread<ST, OP, LES, ODD>(sp, run * 64u + (tid & 31u), yr + off, zb + off);
       }
@@ -109,9 +109,13 @@ void launch3(bool odd, bool plain, bool pairs, unsigned blocks, cudaStream_t s, 
 #define PW_BATCH_LAUNCH(O, P, Q) \
   batch_step<ST, OP, LES, O, P, Q><<<blocks, kBatchThreads, 0, s>>>(params, segs, nsegs, total, lists, counts, rows)
   if (plain) {
-    if (odd) PW_BATCH_LAUNCH(true, true, false);
-    else if (pairs && ST != pw::STORE_F32) PW_BATCH_LAUNCH(false, true, true);
-    else PW_BATCH_LAUNCH(false, true, false);
+    if (pairs && ST != pw::STORE_F32) {
+      if (odd) PW_BATCH_LAUNCH(true, true, true);
+      else PW_BATCH_LAUNCH(false, true, true);
+    } else {
+      if (odd) PW_BATCH_LAUNCH(true, true, false);
+      else PW_BATCH_LAUNCH(false, true, false);
+    }
   } else {
     if (odd) PW_BATCH_LAUNCH(true, false, false);
     else PW_BATCH_LAUNCH(false, false, false);
@@ -148,7 +152,7 @@ struct pw_batch {
   cudaStream_t side = nullptr;    // the seam and edge items, beside the plain items
   cudaEvent_t fork = nullptr, join = nullptr;
   unsigned sms = 1;               // multiprocessors of the device
-  bool pairs = false;             // every member's nx is even: even steps use the cell-pair kernel
+  bool pairs = false;             // every member's nx is even: the plain items use the cell-pair kernel
   const uint32_t **lists = nullptr;
   uint32_t *counts = nullptr;
   uint32_t rows = 4;       // plain rows per work item

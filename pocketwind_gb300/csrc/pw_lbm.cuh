@@ -946,18 +946,26 @@ __global__ void __launch_bounds__(NTHREADS) aa_step_fast(StepParams p) {
 }
 
 // ---------------------------------------------------------------- 16-bit cell pairs
-// The 16-bit storages' plain kernel of even steps: lane t of a warp takes the
-// adjacent cells x0 = 64 r + 2t and x0 + 1 of a 64-cell run r of a row (nx even,
-// so a pair is one aligned 32-bit word of every direction plane).  Even steps
-// touch only the cell's own slots, so each direction is one 32-bit load and
-// one 32-bit store of both cells' codes (whole 128-byte lines per warp), and the
-// store word comes straight out of the paired stochastic conversion.  A word
-// whose two cells are not both stored here (an x-face or wall-link neighbour
-// belongs to the edge kernel) is written half by half.  Odd steps, whose
-// x-shifted directions straddle the word grid, keep the x / x + 32 kernel.
+// The 16-bit storages' plain kernel (nx even): lane t of a warp takes the
+// adjacent cells x0 = 64 r + 2t and x0 + 1 of a 64-cell run r of a row, so a
+// pair is one aligned 32-bit word of every direction plane.  Even steps touch
+// only the cell's own slots: each direction is one 32-bit load and one 32-bit
+// store of both cells' codes (whole 128-byte lines per warp), and the store
+// word comes straight out of the paired stochastic conversion.  On odd steps
+// the directions with c_x = 0 stay on the word grid and move as words; the
+// ten with c_x = +-1 sit one element off it and move as two 16-bit accesses,
+// one per cell (no shuffles, no divergence: 58 memory instructions per pair
+// instead of 76).  A word whose two cells are not both stored here (an
+// x-face or wall-link neighbour belongs to the edge kernel) is written half by
+// half.
 __device__ __forceinline__ uint32_t ld_word(const void *a) {
   uint32_t v;
   asm("ld.global.L2::256B.b32 %0, [%1];" : "=r"(v) : "l"(a));
+  return v;
+}
+__device__ __forceinline__ uint32_t ld_half(const void *a) {
+  unsigned short v;
+  asm("ld.global.b16 %0, [%1];" : "=h"(v) : "l"(a));
   return v;
 }
 __device__ __forceinline__ void st_word(void *a, uint32_t v) {
@@ -973,7 +981,7 @@ __device__ __forceinline__ float raw_of_bits(uint32_t b) {
   return __uint_as_float(b << 16);
 }
 
-template <int ST, int OP, bool LES>
+template <int ST, int OP, bool LES, bool ODD>
 __device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint32_t x, uint32_t y, uint32_t z,
                                            uint32_t ok, uint32_t eq) {
   using S = Store<ST>;
@@ -986,8 +994,13 @@ __device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint
   float2 g[19];
 #pragma unroll
   for (int i = 0; i < 19; i++) {
-    const uint32_t w = ld_word(f + (n + p.ld[i]));
-    g[i] = make_float2(raw_of_bits<ST>(w & 0xffffu), raw_of_bits<ST>(w >> 16));
+    const uint16_t *a = f + (n + p.ld[i]);
+    if (ODD && cx_of(i) != 0) {
+      g[i] = make_float2(raw_of_bits<ST>(ld_half(a)), raw_of_bits<ST>(ld_half(a + 1)));
+    } else {
+      const uint32_t w = ld_word(a);
+      g[i] = make_float2(raw_of_bits<ST>(w & 0xffffu), raw_of_bits<ST>(w >> 16));
+    }
   }
   float2 rho, vx, vy, vz;
   const float2 om = update_fast2<OP, LES>(p, g, rho, vx, vy, vz, S::kScale, S::kInvScale, eq, eux, euy, euz);
@@ -1001,6 +1014,11 @@ __device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint
     for (int j = 0; j < 19; j++) g[j].y = __uint_as_float(0x7fc00000u);
   }
   const uint32_t nk = n * 0x9e3779b9u, nk2 = nk + 0x9e3779b9u;
+  // odd steps: the EQ cell at x = 0 pushes c_x = -1 to x = nx - 1 and the one at
+  // x = nx - 1 pushes c_x = +1 to x = 0 (periodic in x, as idx_wrapped)
+  // (signed element offsets: they are added to the pointer on their own)
+  const int wrap_lo = ODD && (eq & 1u) && x == 0u ? (int)p.nx : 0;
+  const int wrap_hi = ODD && (eq & 2u) && x + 2u == p.nx ? -(int)p.nx : 0;
   // the outlet's upstream cell (x = nx - 2, the first of its pair) publishes the
   // velocity of its stored codes
   const bool pub = (ok & 1u) && x + 2u == p.nx;
@@ -1009,8 +1027,12 @@ __device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint
   for (int j = 0; j < 19; j++) {
     const uint32_t w = S::encode_pair(g[j].y, g[j].x, pair_dither(g[j].y, g[j].x, dither_mul(j), nk2, nk));
     uint16_t *a = f + (n + p.st[j]);
-    if (ok == 3u) st_word(a, w);
-    else {
+    if (ODD && cx_of(j) != 0) {
+      if (ok & 1u) st_half(a + (cx_of(j) < 0 ? wrap_lo : 0), w & 0xffffu);
+      if (ok & 2u) st_half(a + 1 + (cx_of(j) > 0 ? wrap_hi : 0), w >> 16);
+    } else if (ok == 3u) {
+      st_word(a, w);
+    } else {
       if (ok & 1u) st_half(a, w & 0xffffu);
       if (ok & 2u) st_half(a + 1, w >> 16);
     }
@@ -1035,7 +1057,7 @@ __device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint
   }
 }
 
-template <int ST, int OP, bool LES>
+template <int ST, int OP, bool LES, bool ODD>
 __device__ __forceinline__ void pair_thread(const StepParams &p, uint32_t x, uint32_t y, uint32_t z) {
   if (x >= p.nx) return;
   const uint32_t n = x + p.nx * (y + p.ny * z);
@@ -1051,16 +1073,18 @@ __device__ __forceinline__ void pair_thread(const StepParams &p, uint32_t x, uin
       eq |= 1u << k;
     }
   }
-  if (ok) pair_cells<ST, OP, LES>(p, n, x, y, z, ok, eq);
+  if (ok) pair_cells<ST, OP, LES, ODD>(p, n, x, y, z, ok, eq);
 }
 
-// Even steps, one warp per 64-cell run of a row.
-template <int ST, int OP, bool LES>
+// One warp per 64-cell run of a row: every row on even steps, the rows off the
+// periodic y and z seams on odd steps.
+template <int ST, int OP, bool LES, bool ODD>
 __global__ void __launch_bounds__(NTHREADS) aa_step_pairs(StepParams p) {
   const uint32_t x = blockIdx.x * (2 * BX) + 2u * threadIdx.x;
-  const uint32_t y = blockIdx.y * BY + threadIdx.y;
-  if (y >= p.ny) return;
-  pair_thread<ST, OP, LES>(p, x, y, blockIdx.z);
+  const uint32_t y = blockIdx.y * BY + threadIdx.y + (ODD ? 1u : 0u);
+  const uint32_t z = blockIdx.z + (ODD ? 1u : 0u);
+  if (y + (ODD ? 1u : 0u) >= p.ny) return;
+  pair_thread<ST, OP, LES, ODD>(p, x, y, z);
 }
 
 // Odd steps on the seam rows: every row of the planes z = 0 and z = nz-1, then
@@ -1513,12 +1537,19 @@ static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *l
   }
   if (plain) {
     const unsigned runs = (p.nx + 2 * BX - 1) / (2 * BX);  // 64-cell runs per row
-    // even steps of 16-bit storage with whole 32-bit pairs in a row: the pair kernel
+    // 16-bit storage with whole 32-bit pairs in a row: the pair kernel
     const bool pairs = ST != STORE_F32 && (p.nx & 1u) == 0u;
     if (odd) {
       dim3 inner(runs, p.ny > 2u ? (p.ny - 2u + BY - 1u) / BY : 0u, p.nz > 2u ? p.nz - 2u : 0u);
       mark(ev, 0, s);
-      if (inner.y && inner.z) aa_step_fast<ST, OP, LES, true><<<inner, dim3(BX, BY), 0, s>>>(p);
+      if (inner.y && inner.z) {
+        if constexpr (ST != STORE_F32) {
+          if (pairs) aa_step_pairs<ST, OP, LES, true><<<inner, dim3(BX, BY), 0, s>>>(p);
+          else aa_step_fast<ST, OP, LES, true><<<inner, dim3(BX, BY), 0, s>>>(p);
+        } else {
+          aa_step_fast<ST, OP, LES, true><<<inner, dim3(BX, BY), 0, s>>>(p);
+        }
+      }
       mark(ev, 1, s);
       mark(ev, 2, s);
       if (!side) aa_step_seam<ST, OP, LES><<<dim3(g.x, seam_rows(p.ny, p.nz)), BX, 0, s>>>(p);
@@ -1526,7 +1557,7 @@ static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *l
     } else {
       mark(ev, 0, s);
       if constexpr (ST != STORE_F32) {
-        if (pairs) aa_step_pairs<ST, OP, LES><<<dim3(runs, g.y, g.z), dim3(BX, BY), 0, s>>>(p);
+        if (pairs) aa_step_pairs<ST, OP, LES, false><<<dim3(runs, g.y, g.z), dim3(BX, BY), 0, s>>>(p);
         else aa_step_fast<ST, OP, LES, false><<<dim3(runs, g.y, g.z), dim3(BX, BY), 0, s>>>(p);
       } else {
         (void)pairs;
