@@ -15,10 +15,10 @@ e2e     = the same metric through the public solver API the reference's headless
           runner uses (src/app/case-run.ts:154-169): host mesh -> GPU voxelizer ->
           create -> {step 8, encode force, read force} loop, wall clock, with the
           mesh upload (once) and every force readback inside the timed region.
-roofline: the plain-cell kernels (even steps: the 32-bit cell-pair kernel;
-          odd steps: the two-cell x / x+32 kernel and its seam-row variant), all
-          packed FP32 arithmetic, which update all but the wall-link and x-face
-          cells: algorithmic bytes per cell update B = 2 * 19 * s + 1/8
+roofline: the plain-cell kernels (the 32-bit cell-pair kernel, and on odd
+          steps its seam-row variant), packed FP32 arithmetic, which update all
+          but the wall-link and x-face cells: algorithmic bytes per cell update
+          B = 2 * 19 * s + 1/8
           (s = 2 bytes; the 1/8 is the bit-packed special mask), achieved =
           their cells * B / their summed CUDA-event time per step, peak =
           measured HBM copy GB/s.  step_roofline repeats it for whole steps.
@@ -522,8 +522,7 @@ def main():
                    "l2": "inputs larger than L2 (2.5 GB populations)"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                     "kernel": "aa_step_pairs (even steps) + aa_step_fast + aa_step_seam (odd steps): plain cells, "
-                               "two per thread",
+                     "kernel": "aa_step_pairs (+ aa_step_seam on odd steps): plain cells, two per thread",
                      "bytes_per_cell": BYTES["f16"], "cells_per_step": n_plain,
                      "ms_per_step": round(plain_s * 1e3, 4),
                      "traffic": traffic.get("bytes_per_step") if traffic else None,
