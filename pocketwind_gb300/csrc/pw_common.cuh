@@ -189,6 +189,10 @@ struct StepParams {
   // n + ld[i] and stored to element n + st[i] of f, offsets for this step's parity.
   uint32_t ld[19];
   uint32_t st[19];
+  // The same offsets in bytes (element offsets times the element size), added
+  // to a per-thread base pointer by the cell-pair kernel.
+  int64_t ldb[19];
+  int64_t stb[19];
   // Interpolated walls (walls.wgsl:6-21); null qoff means halfway bounce-back.
   // qoff[n]: index of cell n's first wall-link fraction (PW_NO_Q without); q: the
   // fractions in link-rank order; hist: per link, the cell's own post-collision

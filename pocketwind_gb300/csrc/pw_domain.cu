@@ -244,6 +244,8 @@ pw::StepParams params_for(const pw_domain *d, uint64_t step, float u_in, int wri
     const int64_t off = pw::cx_of(i) + nx * pw::cy_of(i) + nxy * pw::cz_of(i);
     p.ld[i] = (uint32_t)(par ? pw::opp_of(i) * S - off : i * S);
     p.st[i] = (uint32_t)(par ? i * S + off : pw::opp_of(i) * S);
+    p.ldb[i] = (int64_t)p.ld[i] * (int64_t)d->esize;
+    p.stb[i] = (int64_t)p.st[i] * (int64_t)d->esize;
   }
   return p;
 }

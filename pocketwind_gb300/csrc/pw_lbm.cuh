@@ -991,10 +991,13 @@ __device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint
     const float4 u = p.plane_in[y + p.ny * z];
     eux.y = u.x; euy.y = u.y; euz.y = u.z;
   }
+  // one 64-bit base per thread; each direction adds its byte offset from the
+  // kernel parameters
+  const char *base = reinterpret_cast<const char *>(f) + 2 * (size_t)n;
   float2 g[19];
 #pragma unroll
   for (int i = 0; i < 19; i++) {
-    const uint16_t *a = f + (n + p.ld[i]);
+    const uint16_t *a = reinterpret_cast<const uint16_t *>(base + p.ldb[i]);
     if (ODD && cx_of(i) != 0) {
       g[i] = make_float2(raw_of_bits<ST>(ld_half(a)), raw_of_bits<ST>(ld_half(a + 1)));
     } else {
@@ -1023,25 +1026,42 @@ __device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint
   // velocity of its stored codes
   const bool pub = (ok & 1u) && x + 2u == p.nx;
   float mass = 1.0f, mx = 0.f, my = 0.f, mz = 0.f;
+  uint32_t w[19];
 #pragma unroll
   for (int j = 0; j < 19; j++) {
-    const uint32_t w = S::encode_pair(g[j].y, g[j].x, pair_dither(g[j].y, g[j].x, dither_mul(j), nk2, nk));
-    uint16_t *a = f + (n + p.st[j]);
-    if (ODD && cx_of(j) != 0) {
-      if (ok & 1u) st_half(a + (cx_of(j) < 0 ? wrap_lo : 0), w & 0xffffu);
-      if (ok & 2u) st_half(a + 1 + (cx_of(j) > 0 ? wrap_hi : 0), w >> 16);
-    } else if (ok == 3u) {
-      st_word(a, w);
-    } else {
-      if (ok & 1u) st_half(a, w & 0xffffu);
-      if (ok & 2u) st_half(a + 1, w >> 16);
-    }
+    w[j] = S::encode_pair(g[j].y, g[j].x, pair_dither(g[j].y, g[j].x, dither_mul(j), nk2, nk));
     if (pub) {
-      const float v = raw_of_bits<ST>(w & 0xffffu) * S::kInvScale;
+      const float v = raw_of_bits<ST>(w[j] & 0xffffu) * S::kInvScale;
       mass += v;
       mx += (float)cx_of(j) * v;
       my += (float)cy_of(j) * v;
       mz += (float)cz_of(j) * v;
+    }
+  }
+  char *obase = reinterpret_cast<char *>(f) + 2 * (size_t)n;
+  if (ok == 3u && !wrap_lo && !wrap_hi) {
+    // both cells stored here (nearly every pair): one branch for all directions
+#pragma unroll
+    for (int j = 0; j < 19; j++) {
+      uint16_t *a = reinterpret_cast<uint16_t *>(obase + p.stb[j]);
+      if (ODD && cx_of(j) != 0) {
+        st_half(a, w[j] & 0xffffu);
+        st_half(a + 1, w[j] >> 16);
+      } else {
+        st_word(a, w[j]);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 19; j++) {
+      uint16_t *a = reinterpret_cast<uint16_t *>(obase + p.stb[j]);
+      if (ODD && cx_of(j) != 0) {
+        if (ok & 1u) st_half(a + (cx_of(j) < 0 ? wrap_lo : 0), w[j] & 0xffffu);
+        if (ok & 2u) st_half(a + 1 + (cx_of(j) > 0 ? wrap_hi : 0), w[j] >> 16);
+      } else {
+        if (ok & 1u) st_half(a, w[j] & 0xffffu);
+        if (ok & 2u) st_half(a + 1, w[j] >> 16);
+      }
     }
   }
   if (pub) {
