@@ -814,7 +814,7 @@ __device__ __forceinline__ void encode_two(float2 v, int j, uint32_t nk, uint32_
     a = S::encode_fast(v.x, dither_mul(j), nk);
     b = S::encode_fast(v.y, dither_mul(j), nk2);
   } else {
-    const uint32_t w = S::encode_pair(v.y, v.x, pair_dither(v.y, v.x, dither_mul(j), nk2, nk));
+    const uint32_t w = S::encode_pair(v.y, v.x, pair_dither<ST>(v.y, v.x, dither_mul(j), nk2, nk));
     if constexpr (ST == STORE_F16) {
       a = __ushort_as_half((unsigned short)(w & 0xffffu));
       b = __ushort_as_half((unsigned short)(w >> 16));
@@ -1029,7 +1029,7 @@ __device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint
   uint32_t w[19];
 #pragma unroll
   for (int j = 0; j < 19; j++) {
-    w[j] = S::encode_pair(g[j].y, g[j].x, pair_dither(g[j].y, g[j].x, dither_mul(j), nk2, nk));
+    w[j] = S::encode_pair(g[j].y, g[j].x, pair_dither<ST>(g[j].y, g[j].x, dither_mul(j), nk2, nk));
     if (pub) {
       const float v = raw_of_bits<ST>(w[j] & 0xffffu) * S::kInvScale;
       mass += v;
