@@ -329,23 +329,28 @@ def batch_leg(steps, sample_steps=200, count=64, peak=None):
     return out
 
 
-def closure_leg(fine_steps, train_steps, threads):
+def closure_leg(fine_steps, train_steps, threads, snapshots=8):
     """The learned closure: fine 256x128x128 vehicle runs (REG + LES + wall model,
-    FP32) at Re 320, 640 and 1280 from seeded 1% velocity perturbations give
-    2x box-filtered samples from the second half of each run; the network trains
-    for `train_steps` Adam steps (batch 65,536, lr 1e-3); the 128x64x64 grid at
-    Re 640 then runs the same physical time with the closure and with plain
-    Smagorinsky.  Drag coefficients (each grid's frontal area) averaged over the
-    last quarter, and device times of the fine and coarse runs."""
+    FP32) at Re 320, 640 and 1280 from seeded 1% velocity perturbations, each
+    `fine_steps` long (20,480 = four flow-throughs by default), give 2x
+    box-filtered samples from `snapshots` snapshots over the last two
+    flow-throughs; the last snapshot of each Re is held out.  The network
+    trains for `train_steps` Adam steps (batch 65,536, lr 1e-3); the 128x64x64
+    grid at Re 640 then runs the same physical time (half the steps) with the
+    closure and with plain Smagorinsky.  Drag coefficients (each grid's frontal
+    area) are averaged over each run's last two flow-throughs, as the
+    reference's validation cases average them (src/validation/cases.ts:101,240),
+    and device times of the fine and coarse runs are compared."""
     import numpy as np
     from pocketwind_gb300 import cases, forces, solver
     from pocketwind_gb300.closure import Closure
     net = Closure(1)
     out = {"fine_grid": "256x128x128", "coarse_grid": "128x64x64", "fine_steps": fine_steps,
-           "train_steps": train_steps, "batch": 65536, "lr": 1e-3}
+           "train_steps": train_steps, "batch": 65536, "lr": 1e-3, "snapshots": snapshots}
     fine_cd = {}
     fine_ms = None
     held = []  # the last snapshot of each Re: held out of training
+    fine_window = min(fine_steps, 2 * forces.flow_through_steps(256))
     for re in (320.0, 640.0, 1280.0):
         v = cases.vehicle_case(256)
         nu_f = 0.05 * v.length_cells / re
@@ -353,21 +358,20 @@ def closure_leg(fine_steps, train_steps, threads):
         s = solver.GpuSolver.create(v.layout, grid, solver.SolverParams(tau0=0.5 + 3 * nu_f, u_in=0.05, les=True,
                                                                          operator="reg"))
         cases.perturbed_start(s, grid, 0.05, 0.01, seed=int(re))
-        half = fine_steps // 2
-        samples = cases.run_drag(s, half)
-        snaps = 4
-        for k in range(snaps):
-            samples += cases.run_drag(s, half // snaps)
+        lead = fine_steps - fine_window
+        samples = cases.run_drag(s, lead) if lead else []
+        per = fine_window // snapshots
+        for k in range(snapshots):
+            samples += cases.run_drag(s, per)
             s.step(1, True)  # a macro step for the snapshot
             start = net.dataset_size
             net.add_samples(s, nu_f / 2)
-            if k == snaps - 1:
+            if k == snapshots - 1:
                 held.append((start, net.dataset_size))
         if re == 640.0:
-            ms = s.time_steps(200)
-            fine_ms = ms / 200
-            tail = [f.fx for f in samples[-len(samples) // 4:]]
-            fine_cd[re] = float(np.mean(tail)) * forces.cd_per_lattice_force(grid.frontal_cells)
+            fx, _, _ = forces.averaged_forces(samples, s.step_count, fine_window)
+            fine_cd[re] = fx * forces.cd_per_lattice_force(grid.frontal_cells)
+            fine_ms = s.time_steps(200) / 200
         s.destroy()
     x, y = net.dataset()
     mask = np.zeros(len(y), bool)
@@ -381,6 +385,8 @@ def closure_leg(fine_steps, train_steps, threads):
     out["a_priori_mse_held_out"] = {"closure": float(np.mean((net.eval(xh) - yh) ** 2)),
                                     "smagorinsky": float(np.mean(yh * yh))}
     coarse = {}
+    coarse_steps = fine_steps // 2
+    coarse_window = min(coarse_steps, 2 * forces.flow_through_steps(128))
     for label, attach in (("closure", True), ("smagorinsky", False)):
         c = cases.vehicle_case(128)
         nu_c = 0.05 * c.length_cells / 640.0
@@ -390,9 +396,9 @@ def closure_leg(fine_steps, train_steps, threads):
         if attach:
             net.attach(s)
         cases.perturbed_start(s, grid, 0.05, 0.01, seed=640)
-        samples = cases.run_drag(s, fine_steps // 2)
-        tail = [f.fx for f in samples[-len(samples) // 4:]]
-        cd = float(np.mean(tail)) * forces.cd_per_lattice_force(grid.frontal_cells)
+        samples = cases.run_drag(s, coarse_steps)
+        fx, _, _ = forces.averaged_forces(samples, coarse_steps, coarse_window)
+        cd = fx * forces.cd_per_lattice_force(grid.frontal_cells)
         ms = s.time_steps(200) / 200
         coarse[label] = {"cd": cd, "ms_per_step": ms, "finite": bool(np.isfinite(s.macros()).all())}
         s.destroy()
@@ -402,6 +408,7 @@ def closure_leg(fine_steps, train_steps, threads):
         # the coarse grid covers the same physical time in half the steps
         coarse[label]["wall_time_ratio_fine_over_coarse"] = (2 * fine_ms) / coarse[label]["ms_per_step"]
     out["fine_cd_re640"] = ref
+    out["average_window_flow_throughs"] = 2
     out["coarse_re640"] = coarse
     net.destroy()
     return out
@@ -441,7 +448,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="profiling runs: skip the end-to-end leg")
     ap.add_argument("--batch-steps", type=int, default=2000,
                     help="steps of the 64-tunnel batched leg (0 skips the leg)")
-    ap.add_argument("--closure-steps", type=int, default=4000,
+    ap.add_argument("--closure-steps", type=int, default=20480,
                     help="fine-grid steps of the learned-closure leg (0 skips the leg)")
     ap.add_argument("--closure-train-steps", type=int, default=20000, help="Adam steps of the closure leg")
     ap.add_argument("--accuracy-steps", type=int, default=1000,
