@@ -56,7 +56,10 @@ enum { PW_OP_TRT = 0, PW_OP_REG = 1 };
 enum { PW_WALLS_BB = 0, PW_WALLS_BOUZIDI = 1 };
 enum { PW_STORE_F32 = 0, PW_STORE_F16 = 1, PW_STORE_BF16 = 2 };
 
-/* SolverParams (src/lbm/gpu-solver.ts:19-30) plus the layout. */
+/* SolverParams (src/lbm/gpu-solver.ts:19-30) plus the layout.  A domain holds
+ * up to 2^32 - 64 cells (the reference's shaders stop at 19 x cells < 2^32,
+ * 226 M cells; here element indices are 64-bit), PW_KERNEL_TILE up to the
+ * reference's limit. */
 typedef struct {
   uint32_t nx, ny, nz;
   double tau0;          /* relaxation time; rounded to binary32 like packSolverParams */
@@ -174,6 +177,11 @@ PW_API int pw_encode_force(pw_domain *dom);
 PW_API int pw_read_force(pw_domain *dom, pw_force_sample *out);
 /* macroBuffer readback: vec4 (rho, ux, uy, uz) per cell, as last written. */
 PW_API int pw_read_macros(pw_domain *dom, float *out);
+/* The macros of the box [x0, x0 + wx) x [y0, y0 + wy) x [z0, z0 + wz), x
+ * fastest, 4 floats per cell, gathered on the GPU: a region of a domain too
+ * large to read whole (no counterpart in the reference). */
+PW_API int pw_read_macros_box(pw_domain *dom, uint32_t x0, uint32_t y0, uint32_t z0, uint32_t wx, uint32_t wy,
+                              uint32_t wz, float *out);
 /* queue.writeBuffer(macroBuffer, ...): replace the macro field (4 floats per
  * cell) that the tracers sample, as the reference's particle test does
  * (tests/browser/particles.spec.ts:54-66). */

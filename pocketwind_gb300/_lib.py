@@ -69,6 +69,7 @@ SIGNATURES = {
     "pw_read_force": (_int, [_vp, C.POINTER(ForceSampleC)]),
     "pw_read_macros": (_int, [_vp, _vp]),
     "pw_write_macros": (_int, [_vp, _vp]),
+    "pw_read_macros_box": (_int, [_vp, _u32, _u32, _u32, _u32, _u32, _u32, _vp]),
     "pw_read_populations": (_int, [_vp, _vp]),
     "pw_read_populations_raw": (_int, [_vp, _vp]),
     "pw_read_populations_noalloc": (_int, [_vp, _vp]),

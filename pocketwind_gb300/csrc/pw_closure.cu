@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(128, 4) closure_step(StepParams p, const uint3
       const pwclosure::Nbr b = pwclosure::make_nbr(p, x, y, z);
       float g[19];
 #pragma unroll
-      for (int i = 0; i < 19; i++) g[i] = S::decode(f[ODD ? b.pull(i, p.stride) : (uint32_t)i * p.stride + n]);
+      for (int i = 0; i < 19; i++) g[i] = S::decode(f[ODD ? b.pull(i, p.stride) : (pw::pidx)i * p.stride + n]);
       float st[11], rho, vx, vy, vz;
       pwclosure::update_fast<OP, true, CaptureHook>(p, g, rho, vx, vy, vz, 1.0f, 1.0f, CaptureHook{st});
       cell_inputs(p, st, (float)wall_dist[n], xin);

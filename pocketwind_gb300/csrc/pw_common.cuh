@@ -11,6 +11,9 @@ namespace pw {
 
 enum : uint32_t { FLUID = 0, SOLID = 1, SUPPORT = 2, FLOOR = 3, EQ = 4 };
 constexpr uint32_t NO_Q = 0xffffffffu;  // cell without packed link fractions
+// Element index into the population array: plane * stride + cell, which passes
+// 2^32 on domains above 226 M cells (cell indices themselves stay below 2^32).
+typedef uint64_t pidx;
 enum : int { STORE_F32 = 0, STORE_F16 = 1, STORE_BF16 = 2 };
 enum : int { OP_TRT = 0, OP_REG = 1 };
 
@@ -191,8 +194,8 @@ struct StepParams {
   uint32_t slip;           // free-slip faces: bit 0 the y faces, bit 1 the z faces (0: periodic)
   // Plain cells (no periodic wrap in reach): direction i is loaded from element
   // n + ld[i] and stored to element n + st[i] of f, offsets for this step's parity.
-  uint32_t ld[19];
-  uint32_t st[19];
+  int64_t ld[19];
+  int64_t st[19];
   // The same offsets in bytes (element offsets times the element size), added
   // to a per-thread base pointer by the cell-pair kernel.
   int64_t ldb[19];

@@ -237,13 +237,13 @@ pw::StepParams params_for(const pw_domain *d, uint64_t step, float u_in, int wri
   // Per-direction element offsets of the plain cells.  Even steps read slot i
   // and write slot opp(j) of the cell itself; odd steps read slot opp(i) of
   // n - c_i and write slot j of n + c_j.  Every offset is non-negative
-  // (stride >= cells) and n + offset < 19 * stride < 2^32.
+  // (stride >= cells) and n + offset < 19 * stride (64-bit element indices).
   const int64_t S = d->stride;
   const int64_t nx = d->nx, nxy = (int64_t)d->nx * d->ny;
   for (int i = 0; i < 19; i++) {
     const int64_t off = pw::cx_of(i) + nx * pw::cy_of(i) + nxy * pw::cz_of(i);
-    p.ld[i] = (uint32_t)(par ? pw::opp_of(i) * S - off : i * S);
-    p.st[i] = (uint32_t)(par ? i * S + off : pw::opp_of(i) * S);
+    p.ld[i] = par ? pw::opp_of(i) * S - off : i * S;
+    p.st[i] = par ? i * S + off : pw::opp_of(i) * S;
     p.ldb[i] = (int64_t)p.ld[i] * (int64_t)d->esize;
     p.stb[i] = (int64_t)p.st[i] * (int64_t)d->esize;
   }
@@ -439,7 +439,9 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
     return PW_ERR_INVALID;
   }
   size_t cells = grid->cells;
-  if (cells * 19 > 0xffffffffull) { set_error("Population buffers exceed u32 shader indexing."); return PW_ERR_INVALID; }
+  // cell indices and the plane stride (cells rounded up to 64) stay 32-bit;
+  // element indices into the population array are 64-bit
+  if (cells > 0xffffffffull - 64) { set_error("The grid exceeds 2^32 cells."); return PW_ERR_INVALID; }
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); set_error("No CUDA device is available."); return PW_ERR_CUDA; }
 
@@ -462,6 +464,11 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
   d->nblocks = (size_t)d->grid.x * d->grid.y * d->grid.z;
   // Staged row tiles: rows must be whole 16-byte multiples for the bulk copies and fit in shared memory.
   if (desc->kernel == PW_KERNEL_TILE) {
+    if ((size_t)19 * d->stride > 0xffffffffull) {
+      set_error("PW_KERNEL_TILE indexes the populations with 32 bits: at most 226 M cells.");
+      delete d;
+      return PW_ERR_INVALID;
+    }
     if ((d->nx * d->esize) % 16 != 0) {
       set_error("PW_KERNEL_TILE needs nx * element bytes to be a multiple of 16.");
       delete d;
@@ -881,6 +888,16 @@ extern "C" int pw_closure_attach(pw_domain *d, const pw_closure *c) {
 // ---------------------------------------------------------------- field export, checkpoint
 namespace {
 
+// The macros of a box of cells, x fastest, into a packed device buffer.
+__global__ void macro_box_kernel(const float4 *macros, uint32_t nx, uint32_t ny, uint32_t x0, uint32_t y0,
+                                 uint32_t z0, uint32_t wx, uint32_t wy, uint32_t wz, float4 *out) {
+  const size_t total = (size_t)wx * wy * wz;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
+    const size_t x = k % wx, y = (k / wx) % wy, z = k / ((size_t)wx * wy);
+    out[k] = macros[(x0 + x) + (size_t)nx * ((y0 + y) + (size_t)ny * (z0 + z))];
+  }
+}
+
 __device__ __forceinline__ uint32_t big_endian(float v) { return __byte_perm(__float_as_uint(v), 0u, 0x0123u); }
 
 // The bytes of writeVtk (src/io/vtk.ts:56-80) after the header, with latticeToField's
@@ -985,6 +1002,27 @@ int pw_field_vtk_body(pw_domain *d, double velocity_scale, void *out, size_t cap
   PW_TRY(cudaGetLastError());
   PW_TRY(cudaMemcpyAsync(out, d->scratch, bytes, cudaMemcpyDeviceToHost, d->stream));
   PW_TRY(cudaStreamSynchronize(d->stream));
+  return PW_OK;
+}
+
+int pw_read_macros_box(pw_domain *d, uint32_t x0, uint32_t y0, uint32_t z0, uint32_t wx, uint32_t wy, uint32_t wz,
+                       float *out) {
+  if (!alive(d) || !out) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  if (wx == 0 || wy == 0 || wz == 0 || (uint64_t)x0 + wx > d->nx || (uint64_t)y0 + wy > d->ny ||
+      (uint64_t)z0 + wz > d->nz) {
+    set_error("The box must be non-empty and inside the grid.");
+    return PW_ERR_INVALID;
+  }
+  const size_t total = (size_t)wx * wy * wz;
+  float4 *buf = nullptr;
+  PW_TRY(cudaMallocAsync((void **)&buf, total * sizeof(float4), d->stream));
+  unsigned blocks = (unsigned)std::min<size_t>((total + 255) / 256, (size_t)152 * 16);
+  macro_box_kernel<<<blocks, 256, 0, d->stream>>>(d->macros, d->nx, d->ny, x0, y0, z0, wx, wy, wz, buf);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, buf, total * sizeof(float4), cudaMemcpyDeviceToHost, d->stream);
+  cudaFreeAsync(buf, d->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(d->stream);
+  if (e != cudaSuccess) return cuda_status(e, "pw_read_macros_box");
   return PW_OK;
 }
 

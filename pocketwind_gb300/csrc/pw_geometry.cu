@@ -658,8 +658,8 @@ int pw_voxelize_opts(const float *body, uint32_t body_triangles, const float *su
     return PW_ERR_INVALID;
   }
   size_t cells = (size_t)nx * ny * nz;
-  if (cells * 19 > 0xffffffffull) {
-    set_error("Population buffers exceed u32 indexing.");
+  if (cells > 0xffffffffull - 64) {
+    set_error("The grid exceeds 2^32 cells.");
     return PW_ERR_INVALID;
   }
   if ((body_triangles && !body) || (support_triangles && !supports)) {
@@ -712,7 +712,7 @@ int pw_grid_from_host(uint32_t nx, uint32_t ny, uint32_t nz, const uint32_t *geo
   *out = nullptr;
   if (nx < 1 || ny < 1 || nz < 1) { set_error("Grid dimensions must be positive safe integers."); return PW_ERR_INVALID; }
   size_t cells = (size_t)nx * ny * nz;
-  if (cells * 19 > 0xffffffffull) { set_error("Population buffers exceed u32 indexing."); return PW_ERR_INVALID; }
+  if (cells > 0xffffffffull - 64) { set_error("The grid exceeds 2^32 cells."); return PW_ERR_INVALID; }
   if (!geometry || geometry_len < 2 * cells) {
     set_error("Geometry must match the solver layout and contain flags and q offsets.");
     return PW_ERR_INVALID;

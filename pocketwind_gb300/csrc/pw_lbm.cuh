@@ -464,22 +464,22 @@ struct Nbr {
   // Odd steps push P(j, n) into slot j of n + c_j; across a free-slip face the
   // population reflects: slot mirror(j) of the in-plane neighbour.  This is also
   // where P(j, n) sits after an odd step (the readout map).
-  __device__ __forceinline__ uint32_t push(int j, uint32_t stride) const {
+  __device__ __forceinline__ pidx push(int j, uint32_t stride) const {
     const int cy = cy_of(j), cz = cz_of(j);
     const bool ry = (cy > 0 && syp) || (cy < 0 && sym);
     const bool rz = (cz > 0 && szp) || (cz < 0 && szm);
     const int k = ry ? (rz ? mirror_yz(j) : mirror_y(j)) : (rz ? mirror_z(j) : j);
-    return (uint32_t)k * stride + at(cx_of(j), ry ? 0 : cy, rz ? 0 : cz);
+    return (pidx)k * stride + at(cx_of(j), ry ? 0 : cy, rz ? 0 : cz);
   }
   // Odd steps pull direction i from slot opp(i) of n - c_i; across a free-slip
   // face from slot opp(mirror(i)) of the in-plane neighbour, where that
   // neighbour's even step left P(mirror(i)).
-  __device__ __forceinline__ uint32_t pull(int i, uint32_t stride) const {
+  __device__ __forceinline__ pidx pull(int i, uint32_t stride) const {
     const int cy = -cy_of(i), cz = -cz_of(i);
     const bool ry = (cy > 0 && syp) || (cy < 0 && sym);
     const bool rz = (cz > 0 && szp) || (cz < 0 && szm);
     const int k = ry ? (rz ? mirror_yz(i) : mirror_y(i)) : (rz ? mirror_z(i) : i);
-    return (uint32_t)opp_of(k) * stride + at(-cx_of(i), ry ? 0 : cy, rz ? 0 : cz);
+    return (pidx)opp_of(k) * stride + at(-cx_of(i), ry ? 0 : cy, rz ? 0 : cz);
   }
 };
 
@@ -504,9 +504,9 @@ __device__ __forceinline__ Nbr make_nbr(const StepParams &p, uint32_t x, uint32_
 
 // Location of P(j, n) after a step of the given parity (the readout map).
 template <bool ODD_LAYOUT>
-__device__ __forceinline__ uint32_t slot_of(const Nbr &b, int j, uint32_t stride, uint32_t n) {
+__device__ __forceinline__ pidx slot_of(const Nbr &b, int j, uint32_t stride, uint32_t n) {
   if (ODD_LAYOUT) return b.push(j, stride);
-  return (uint32_t)opp_of(j) * stride + n;
+  return (pidx)opp_of(j) * stride + n;
 }
 
 // The velocity the outlet takes from its upstream cell: stream_collide.wgsl:83-93
@@ -637,12 +637,12 @@ __device__ __forceinline__ void general_cell(const StepParams &p, uint32_t x, ui
     float g[19];
 #pragma unroll
     for (int i = 0; i < 19; i++) {
-      uint32_t src;
+      pidx src;
       if (ODD) src = b.pull(i, S_);
-      else src = (uint32_t)i * S_ + n;
+      else src = (pidx)i * S_ + n;
       if (i > 0 && (flag & (1u << (3 + i)))) {  // wall link i: the slot nobody rewrites this step
-        if (ODD) src = (uint32_t)i * S_ + n;
-        else src = (uint32_t)opp_of(i) * S_ + b.at(-cx_of(i), -cy_of(i), -cz_of(i));
+        if (ODD) src = (pidx)i * S_ + n;
+        else src = (pidx)opp_of(i) * S_ + b.at(-cx_of(i), -cy_of(i), -cz_of(i));
       }
       g[i] = S::decode(f[src]);
     }
@@ -670,9 +670,9 @@ __device__ __forceinline__ void general_cell(const StepParams &p, uint32_t x, ui
   for (int j = 0; j < 19; j++) code[j] = S::encode(post[j], (uint32_t)j, n);
 #pragma unroll
   for (int j = 0; j < 19; j++) {
-    uint32_t dst;
+    pidx dst;
     if (ODD) dst = b.push(j, S_);
-    else dst = (uint32_t)opp_of(j) * S_ + n;
+    else dst = (pidx)opp_of(j) * S_ + n;
     f[dst] = code[j];
   }
   if (p.qoff != nullptr && (flag >> 3) != 0u) {
@@ -737,7 +737,7 @@ __global__ void __launch_bounds__(NTHREADS) aa_step(StepParams p) {
 // through general_cell and owns the force.
 template <int ST, int OP, bool LES, bool ODD>
 __device__ __forceinline__ void plain_cell(const StepParams &p, uint32_t n, uint32_t x, uint32_t y, uint32_t z,
-                                           const uint32_t *ld, const uint32_t *st) {
+                                           const int64_t *ld, const int64_t *st) {
   using S = Store<ST>;
   using T = typename S::T;
   T *f = reinterpret_cast<T *>(p.f);
@@ -781,7 +781,7 @@ __device__ __forceinline__ void plain_cell(const StepParams &p, uint32_t n, uint
 // as in general_cell, stored through the seam kernel's wrapped offsets st.
 template <int ST, bool ODD>
 __device__ __forceinline__ void eq_cell(const StepParams &p, uint32_t n, uint32_t x, uint32_t y, uint32_t z,
-                                        const uint32_t *st) {
+                                        const int64_t *st) {
   using S = Store<ST>;
   using T = typename S::T;
   T *f = reinterpret_cast<T *>(p.f);
@@ -886,8 +886,9 @@ __device__ __forceinline__ void plain_pair(const StepParams &p, uint32_t n, uint
     const uint32_t xa = x, xb = x + 32u;
 #pragma unroll
     for (int j = 0; j < 19; j++) {
-      const uint32_t wa = cx_of(j) < 0 && xa == 0u ? p.nx : (cx_of(j) > 0 && xa + 1u == p.nx ? 0u - p.nx : 0u);
-      const uint32_t wb = cx_of(j) > 0 && xb + 1u == p.nx ? 0u - p.nx : 0u;
+      // signed: added to 64-bit element indices
+      const int64_t wa = cx_of(j) < 0 && xa == 0u ? (int64_t)p.nx : (cx_of(j) > 0 && xa + 1u == p.nx ? -(int64_t)p.nx : 0);
+      const int64_t wb = cx_of(j) > 0 && xb + 1u == p.nx ? -(int64_t)p.nx : 0;
       T ca, cb;
       encode_two<ST>(g[j], j, nk, nk2, ca, cb);
       if (ok & 1u) f[n + p.st[j] + wa] = ca;
@@ -1134,11 +1135,11 @@ __device__ __forceinline__ void seam_thread(const StepParams &p, uint32_t x, uin
   if (special ? __ldg(&p.flags[n]) != EQ : !is_plain_position(x, p.nx)) return;
   // offsets relative to n of the wrapped (or reflected, on free-slip faces) slots
   const Nbr b = make_nbr(p, x, y, z);
-  uint32_t ld[19], st[19];
+  int64_t ld[19], st[19];
 #pragma unroll
   for (int i = 0; i < 19; i++) {
-    ld[i] = b.pull(i, p.stride) - n;
-    st[i] = b.push(i, p.stride) - n;
+    ld[i] = (int64_t)b.pull(i, p.stride) - (int64_t)n;
+    st[i] = (int64_t)b.push(i, p.stride) - (int64_t)n;
   }
   if (special) eq_cell<ST, true>(p, n, x, y, z, st);
   else plain_cell<ST, OP, LES, true>(p, n, x, y, z, ld, st);
@@ -1198,7 +1199,7 @@ __device__ __forceinline__ void init_cell(const StepParams &p, uint32_t x, uint3
   for (int j = 0; j < 19; j++) code[j] = S::encode(geq_ref(j, 0.0f, vx, 0.f, 0.f), (uint32_t)j, n);
   if (!is_wall_kind(kind)) {
 #pragma unroll
-    for (int j = 0; j < 19; j++) f[(uint32_t)opp_of(j) * p.stride + n] = code[j];
+    for (int j = 0; j < 19; j++) f[(pidx)opp_of(j) * p.stride + n] = code[j];
     if (kind == FLUID && (flag >> 3)) {
 #pragma unroll
       for (int i = 1; i < 19; i++) {
@@ -1428,9 +1429,9 @@ __device__ __forceinline__ void interpolated_state_cell(const StepParams &p, int
   float g[19];
 #pragma unroll
   for (int i = 0; i < 19; i++) {
-    uint32_t src = odd_layout ? (uint32_t)i * S_ + n : b.pull(i, S_);
+    pidx src = odd_layout ? (pidx)i * S_ + n : b.pull(i, S_);
     if (i > 0 && (flag & (1u << (3 + i))))
-      src = odd_layout ? (uint32_t)opp_of(i) * S_ + b.at(-cx_of(i), -cy_of(i), -cz_of(i)) : (uint32_t)i * S_ + n;
+      src = odd_layout ? (pidx)opp_of(i) * S_ + b.at(-cx_of(i), -cy_of(i), -cz_of(i)) : (pidx)i * S_ + n;
     g[i] = S::decode(f[src]);
   }
   interpolated_links(p, b, n, flag, g, OwnFromHist<ST>{hist}, fx, fy, fz, any);

@@ -79,7 +79,7 @@ __global__ void read_slab_kernel(pw::StepParams p, int odd_layout, int j, uint32
   float v = 0.0f;
   if (!pw::is_wall_kind(p.flags[n] & 7u)) {
     const pwnoalloc::Nbr b = pwnoalloc::make_nbr(p, x, y, z);
-    uint32_t k = odd_layout ? pwnoalloc::slot_of<true>(b, j, p.stride, n)
+    pw::pidx k = odd_layout ? pwnoalloc::slot_of<true>(b, j, p.stride, n)
                             : pwnoalloc::slot_of<false>(b, j, p.stride, n);
     v = S::decode(f[k]);
   }

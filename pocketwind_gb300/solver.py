@@ -153,6 +153,15 @@ class GpuSolver:
         _lib.check(_lib.load().pw_read_macros(self._live(), out.ctypes.data_as(C.c_void_p)), "macros")
         return out
 
+    def macros_box(self, origin, size) -> np.ndarray:
+        """Macros (rho, ux, uy, uz) of a box of cells, shape (wz, wy, wx, 4)."""
+        x0, y0, z0 = (int(v) for v in origin)
+        wx, wy, wz = (int(v) for v in size)
+        out = np.empty((wz, wy, wx, 4), np.float32)
+        _lib.check(_lib.load().pw_read_macros_box(self._live(), x0, y0, z0, wx, wy, wz,
+                                                  out.ctypes.data_as(C.c_void_p)), "macros_box")
+        return out
+
     def write_macros(self, macros: np.ndarray) -> None:
         a = np.ascontiguousarray(macros, np.float32).reshape(-1)
         if a.size != 4 * self.cells:
