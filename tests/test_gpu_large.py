@@ -52,4 +52,4 @@ def test_large_domain_matches_small_domain(precision):
         assert np.array_equal(big.view(np.uint32), small.view(np.uint32))
     else:
         moved = _run(SMALL, 40, 24, precision)  # the same flow on other cells: another dither realization
-        assert _du(big, small) < 2 * _du(moved, small) + 1e-3
+        assert _du(big, small) < 3 * _du(moved, small) + 1e-3
