@@ -454,16 +454,16 @@ int pw_batch_time_steps(pw_batch *b, uint64_t count, float *ms) {
   return PW_OK;
 }
 
-// Time every candidate launch shape (persistent grid of 1, 2, 4, 8 or 16 blocks
-// per SM, and 4, 8 or 16 plain rows per work item) over `trial_steps` real
+// Time every candidate launch shape (persistent grid of 2, 4, 8, 16 or 32 blocks
+// per SM, and 8, 16, 32 or 64 plain rows per work item) over `trial_steps` real
 // steps each (an even number, after two warm-up steps) and keep the fastest.
 // The trial steps advance the members.
 int pw_batch_tune(pw_batch *b, uint32_t trial_steps, pw_batch_tuning *out) {
   if (!b || trial_steps == 0) { set_error("The batch handle is NULL or the trial has no steps."); return PW_ERR_INVALID; }
   trial_steps += trial_steps & 1u;
   const unsigned sms = (unsigned)max_blocks();
-  const unsigned grid_mult[] = {1, 2, 4, 8, 16};
-  const uint32_t row_opts[] = {4, 8, 16};
+  const unsigned grid_mult[] = {2, 4, 8, 16, 32};
+  const uint32_t row_opts[] = {8, 16, 32, 64};
   float best = 1e30f;
   unsigned best_blocks = b->blocks;
   uint32_t best_rows = b->rows, tried = 0;

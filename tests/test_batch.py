@@ -76,7 +76,7 @@ def test_tuning_keeps_a_working_shape_and_reset_restarts():
     members = [_make(t, "f16") for t in tunnels]
     batch = Batch(members)
     t = batch.tune(4)
-    assert t.candidates == 15 and t.rows_per_item in (4, 8, 16) and t.blocks > 0 and t.ms_per_step > 0
+    assert t.candidates == 20 and t.rows_per_item in (8, 16, 32, 64) and t.blocks > 0 and t.ms_per_step > 0
     batch.reset()
     solo = [_make(x, "f16") for x in tunnels]
     batch.step(20, True)
