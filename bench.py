@@ -27,6 +27,8 @@ cpu_baseline: the binary64 restatement of the reference's CpuSolver (the
           host cores, over a bounded number of full-domain steps.
 accuracy: drag and field errors against that binary64 restatement: the sphere
           at Re 100 (96x48x48, FP32) and the 128x64x64 vehicle in each storage.
+grid_check: the reference's three-tier grid check (GCI band) run one tier
+          after another and with the three tiers side by side on one GPU;
 batched_tunnels: 64 seeded tunnels of uneven size and Re, FP16 TRT, two
           concurrent persistent launches per step from captured graphs,
           autotuned shape;
@@ -414,6 +416,33 @@ def closure_leg(fine_steps, train_steps, threads, snapshots=8):
     return out
 
 
+def grid_check_leg(run_flow_throughs):
+    """The grid check (src/app/grid-check.ts): the sphere preset at a body
+    length of 16 cells on tier S (128x64x64), 24 on M, 32 on L, Re 100 on the
+    body length, REG + LES, FP16, `run_flow_throughs` flow-throughs per tier
+    with the newest half averaged.  Wall time of the reference's order (one tier
+    after another) against the three tiers stepped side by side on one GPU,
+    and the band they give."""
+    from pocketwind_gb300 import meshes, reporting
+
+    def sphere_for(length, layout):
+        return meshes.place_mesh(meshes.preset_mesh("sphere"), *layout, length, False)
+
+    t0 = time.perf_counter()
+    seq = reporting.run_grid_check(16, 128, reporting.gpu_tier_runner(sphere_for, re=100.0, floor=False),
+                                   run_flow_throughs=run_flow_throughs)
+    t1 = time.perf_counter()
+    conc = reporting.gpu_grid_check(sphere_for, 16, 128, re=100.0, run_flow_throughs=run_flow_throughs, floor=False)
+    t2 = time.perf_counter()
+    band = conc.band
+    return {"body": "sphere preset", "lengths_cells": [r.length_cells for r in conc.rows],
+            "cd": [r.cd for r in conc.rows], "flow_throughs": run_flow_throughs,
+            "band": ({"gci_pct": band.gci_pct, "extrapolated_cd": band.extrapolated_cd} if band.kind == "band"
+                     else {"no_band": band.reason}),
+            "rows_equal_one_at_a_time": conc.rows == seq.rows,
+            "seconds_one_at_a_time": round(t1 - t0, 3), "seconds_side_by_side": round(t2 - t1, 3)}
+
+
 def cell_classes(flags):
     """Cells updated per step by the plain-cell kernels (plain fluid with
     1 <= x <= nx-2, and EQ cells without wall links) and by the edge kernel."""
@@ -451,6 +480,8 @@ def main():
     ap.add_argument("--closure-steps", type=int, default=20480,
                     help="fine-grid steps of the learned-closure leg (0 skips the leg)")
     ap.add_argument("--closure-train-steps", type=int, default=20000, help="Adam steps of the closure leg")
+    ap.add_argument("--grid-check-flow-throughs", type=float, default=4,
+                    help="flow-throughs per tier of the grid-check leg (0 skips the leg)")
     ap.add_argument("--accuracy-steps", type=int, default=1000,
                     help="vehicle steps of the accuracy leg against FP64 (0 skips the leg)")
     args = ap.parse_args()
@@ -555,6 +586,8 @@ def main():
         line["batched_tunnels"] = batch_leg(args.batch_steps, peak=peak)
     if world == 1 and args.closure_steps > 0:
         line["learned_closure"] = closure_leg(args.closure_steps, args.closure_train_steps, os.cpu_count() or 1)
+    if world == 1 and args.grid_check_flow_throughs > 0:
+        line["grid_check"] = grid_check_leg(args.grid_check_flow_throughs)
     if world == 1 and args.accuracy_steps > 0:
         line["accuracy"] = accuracy_leg(args.accuracy_steps, os.cpu_count() or 1)
     if world == 1 and args.cpu_steps > 0:
