@@ -27,6 +27,8 @@ cpu_baseline: the binary64 restatement of the reference's CpuSolver (the
           host cores, over a bounded number of full-domain steps.
 accuracy: drag and field errors against that binary64 restatement: the sphere
           at Re 100 (96x48x48, FP32) and the 128x64x64 vehicle in each storage.
+tracers:  the 128x64x64 vehicle in frames of 8 steps with 3-D streaklines, the
+          plate smoke and particles advanced after each frame; device times;
 grid_check: the reference's three-tier grid check (GCI band) run one tier
           after another and with the three tiers side by side on one GPU;
 batched_tunnels: 64 seeded tunnels of uneven size and Re, FP16 TRT, two
@@ -443,6 +445,85 @@ def grid_check_leg(run_flow_throughs):
             "seconds_one_at_a_time": round(t1 - t0, 3), "seconds_side_by_side": round(t2 - t1, 3)}
 
 
+def tracer_leg(steps):
+    """The tracers on the 128x64x64 vehicle (FP32, REG + LES, floor on), stepped
+    in frames of 8 steps as the reference's frame loop does (src/app/run.ts:42,
+    345), the macros written on each frame's last step.  After every frame: a
+    16x16 rake of 3-D streaklines at x = 2 (512 puffs per nozzle), the plate
+    smoke on the centre plane (36 rake threads and the 6 dye ports placed on
+    the voxelized body, 8192 ring slots each; src/render/plate.ts:522-548) and
+    65,536 particles seeded at x = 2 (src/render/particles.ts).  CUDA events
+    on the domain's stream (torch.cuda.ExternalStream) time the frame's steps
+    and each tracer kernel."""
+    import numpy as np
+    import torch
+    from pocketwind_gb300 import cases, particle_layout as PAL, plate_layout as PL
+    from pocketwind_gb300.solver import GpuSolver
+    from pocketwind_gb300.tracers import Particles, PlateSmoke, Streaks
+
+    case = cases.vehicle_case(128)
+    grid = case.grid()
+    layout = case.layout
+    s = GpuSolver.create(layout, grid, case.params("f32"))
+    if isinstance(s, Exception):
+        raise s
+    plane = layout[1] // 2
+    pts = case.body.positions.reshape(-1, 3)
+    # a desktop plate shows the whole z span that fitPlate gives it (plate-layout.ts:69)
+    z_top = min(layout[2] - 2, max(1.9 * float(pts[:, 2].max()), 0.45 * layout[2]))
+    low, high = PL.rake_span(z_top, layout[2])
+    ports = PL.dye_ports(grid.flags, layout, plane, (low, high)).reshape(-1, 2)
+    streaks = Streaks(s, 16, 16, 512, (2.0, 16.0, 48.0, 1.5, 30.0))
+    plate = PlateSmoke(s, plane, PL.RAKE_THREADS, 8192, ports)
+    seeds, region, fallback = PAL.particle_seeds(grid.flags, layout, pts.min(axis=0), pts.max(axis=0), 65536, 7)
+    particles = Particles(s, seeds, 7, region, fallback)
+    stream = torch.cuda.ExternalStream(s.buffers()[2])
+    frames = max(1, steps // 8)
+    total = np.zeros(4)
+    rake = (float(PL.RAKE_X), low, high, 8.0)
+    chunk = 50  # frames queued between host waits, so the host runs ahead of the device
+    pending = []
+    for frame in range(frames):
+        release, releasing = frame // 2, frame % 2 == 0
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+        ev[0].record(stream)
+        s.step(8, True)
+        ev[1].record(stream)
+        streaks.advance(8.0, release, releasing)
+        ev[2].record(stream)
+        plate.advance(release, releasing, rake)
+        ev[3].record(stream)
+        particles.update(8.0)
+        ev[4].record(stream)
+        if frame >= 8:  # the first frames warm the kernels up
+            pending.append(ev)
+        if len(pending) == chunk or frame == frames - 1:
+            for e in pending:
+                e[4].synchronize()
+                total += [e[k].elapsed_time(e[k + 1]) for k in range(4)]
+            pending = []
+    timed = frames - min(frames, 8)
+    puffs, _ = streaks.read()
+    smoke = plate.read()
+    recs = particles.read()
+    unstable = s.guard_unstable()
+    per = total / max(1, timed)
+    out = {"case": "vehicle 128x64x64, FP32, REG + LES, floor", "frames": frames, "steps_per_frame": 8,
+           "ms_per_frame": {"steps": per[0], "streaks": per[1], "plate_smoke": per[2], "particles": per[3]},
+           "tracer_share_of_frame": float(per[1:].sum() / per.sum()) if per.sum() > 0 else None,
+           "streaks": {"puffs": streaks.n, "live": int((puffs[:, 3] > 0).sum()),
+                       "puff_advances_per_s": streaks.n / (per[1] * 1e-3) if per[1] > 0 else None},
+           "plate_smoke": {"slots": int(smoke.shape[0]), "live": int((smoke[:, 3] > 0).sum()),
+                           "slot_advances_per_s": smoke.shape[0] / (per[2] * 1e-3) if per[2] > 0 else None},
+           "particles": {"count": int(recs.shape[0]), "finite": bool(np.isfinite(recs).all()),
+                         "updates_per_s": recs.shape[0] / (per[3] * 1e-3) if per[3] > 0 else None},
+           "unstable": unstable}
+    for t in (particles, plate, streaks):
+        t.destroy()
+    s.destroy()
+    return out
+
+
 def cell_classes(flags):
     """Cells updated per step by the plain-cell kernels (plain fluid with
     1 <= x <= nx-2, and EQ cells without wall links) and by the edge kernel."""
@@ -480,6 +561,8 @@ def main():
     ap.add_argument("--closure-steps", type=int, default=20480,
                     help="fine-grid steps of the learned-closure leg (0 skips the leg)")
     ap.add_argument("--closure-train-steps", type=int, default=20000, help="Adam steps of the closure leg")
+    ap.add_argument("--tracer-steps", type=int, default=20000,
+                    help="solver steps of the tracer leg, 8 per frame (0 skips the leg)")
     ap.add_argument("--grid-check-flow-throughs", type=float, default=4,
                     help="flow-throughs per tier of the grid-check leg (0 skips the leg)")
     ap.add_argument("--accuracy-steps", type=int, default=1000,
@@ -586,6 +669,8 @@ def main():
         line["batched_tunnels"] = batch_leg(args.batch_steps, peak=peak)
     if world == 1 and args.closure_steps > 0:
         line["learned_closure"] = closure_leg(args.closure_steps, args.closure_train_steps, os.cpu_count() or 1)
+    if world == 1 and args.tracer_steps > 0:
+        line["tracers"] = tracer_leg(args.tracer_steps)
     if world == 1 and args.grid_check_flow_throughs > 0:
         line["grid_check"] = grid_check_leg(args.grid_check_flow_throughs)
     if world == 1 and args.accuracy_steps > 0:
