@@ -344,10 +344,12 @@ def closure_leg(fine_steps, train_steps, threads, snapshots=8):
     closure and with plain Smagorinsky.  Drag coefficients (each grid's frontal
     area) are averaged over each run's last two flow-throughs, as the
     reference's validation cases average them (src/validation/cases.ts:101,240),
-    and device times of the fine and coarse runs are compared."""
+    and device times of the fine and coarse runs are compared.  A third coarse
+    run without the plain cells' eddy viscosity gives the floor that no closure
+    of this form can go below."""
     import numpy as np
     from pocketwind_gb300 import cases, forces, solver
-    from pocketwind_gb300.closure import Closure
+    from pocketwind_gb300.closure import N_PARAMS, Closure
     net = Closure(1)
     out = {"fine_grid": "256x128x128", "coarse_grid": "128x64x64", "fine_steps": fine_steps,
            "train_steps": train_steps, "batch": 65536, "lr": 1e-3, "snapshots": snapshots}
@@ -391,14 +393,20 @@ def closure_leg(fine_steps, train_steps, threads, snapshots=8):
     coarse = {}
     coarse_steps = fine_steps // 2
     coarse_window = min(coarse_steps, 2 * forces.flow_through_steps(128))
-    for label, attach in (("closure", True), ("smagorinsky", False)):
+    # the floor of any closure that only scales the plain cells' eddy viscosity
+    # by max(0, 1 + c): zero weights and output bias -1 remove it
+    floor_net = Closure(1)
+    w = np.zeros(N_PARAMS, np.float32)
+    w[-1] = -1.0
+    floor_net.params = w
+    for label, attach in (("closure", net), ("smagorinsky", None), ("no_eddy_viscosity", floor_net)):
         c = cases.vehicle_case(128)
         nu_c = 0.05 * c.length_cells / 640.0
         grid = c.grid()
         s = solver.GpuSolver.create(c.layout, grid, solver.SolverParams(tau0=0.5 + 3 * nu_c, u_in=0.05, les=True,
                                                                          operator="reg"))
-        if attach:
-            net.attach(s)
+        if attach is not None:
+            attach.attach(s)
         cases.perturbed_start(s, grid, 0.05, 0.01, seed=640)
         samples = cases.run_drag(s, coarse_steps)
         fx, _, _ = forces.averaged_forces(samples, coarse_steps, coarse_window)
@@ -415,6 +423,7 @@ def closure_leg(fine_steps, train_steps, threads, snapshots=8):
     out["average_window_flow_throughs"] = 2
     out["coarse_re640"] = coarse
     net.destroy()
+    floor_net.destroy()
     return out
 
 
