@@ -140,6 +140,31 @@ class ClockSampler:
         return out
 
 
+def barrier(world):
+    """All ranks meet here (replica runs); a no-op on one GPU."""
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(values, world):
+    """Each value's maximum over the ranks: the slowest replica sets the job's time."""
+    if world == 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def job_mlups(cells, steps, world, ms):
+    """Whole-job MLUPS of `world` replicas that each updated `cells` cells
+    `steps` times, the slowest taking `ms` milliseconds."""
+    return cells * steps * world / (ms * 1e3)
+
+
 def build_case():
     from pocketwind_gb300 import meshes
     return meshes.vehicle_case_mesh(NX, NY, SCALE)
@@ -167,7 +192,9 @@ def run_ours(args, rank, world):
         if precision == "f16":
             sampler = ClockSampler()
             sampler.start()
+        barrier(world)
         ms = solver.time_steps(args.steps)
+        barrier(world)
         if precision == "f16":
             clocks = sampler.stop()
         kernel_ms = solver.profile_steps(min(args.steps, 200)) if precision == "f16" else None
@@ -181,6 +208,7 @@ def run_ours(args, rank, world):
         return results, None, 0, body.positions.nbytes, cells, grid
     # end-to-end through the public API (wall clock): mesh upload + voxelize + create + sampled stepping
     import time as _t
+    barrier(world)
     t0 = _t.perf_counter()
     grid2 = voxelize(body, None, (NX, NY, NZ), True)
     solver = GpuSolver.create((NX, NY, NZ), grid2, SolverParams(tau0=TAU0, u_in=U_IN, les=True, operator="reg",
@@ -191,6 +219,7 @@ def run_ours(args, rank, world):
         solver.encode_force()
         f = solver.read_force()
     e2e_s = _t.perf_counter() - t0
+    barrier(world)
     solver.destroy()
     e2e_steps = samples * 8
     return results, e2e_s, e2e_steps, body.positions.nbytes, cells, grid
@@ -613,17 +642,12 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
     results, e2e_s, e2e_steps, mesh_bytes, cells, grid = run_ours(args, rank, world)
-    ms = results["f16"]["ms"]
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms, e2e_max = max_over_ranks([results["f16"]["ms"], e2e_s or 0.0], world)
+    e2e_s = e2e_max if e2e_s else None
     if rank != 0:
         return
     peak, peak_kind = read_peaks()
-    mlups = cells * args.steps * world / (ms * 1e3)
+    mlups = job_mlups(cells, args.steps, world, ms)
     step_achieved = cells * BYTES["f16"] / (ms / args.steps / 1e3) / 1e9
     n_plain, n_edge = cell_classes(grid.flags)
     kms = results["f16"]["kernel_ms"]
@@ -665,7 +689,7 @@ def main():
                               "hbm_frac": round(cells * BYTES[p] / (r["ms"] / args.steps / 1e3) / 1e9 / peak, 4),
                               "stable": not r["unstable"]}
                           for p, r in results.items()},
-        "e2e": ({"value": round(cells * e2e_steps / (e2e_s * 1e6), 2), "unit": "MLUPS",
+        "e2e": ({"value": round(job_mlups(cells, e2e_steps, world, e2e_s * 1e3), 2), "unit": "MLUPS",
                  "h2d_bytes_per_step": round(mesh_bytes / e2e_steps, 2),
                  "d2h_bytes_per_step": round(24 / 8, 2)} if e2e_s else None),
         "gpu_launches": launches,
