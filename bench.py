@@ -679,6 +679,9 @@ def main():
                      "kernel": "aa_step_pairs (+ aa_step_seam on odd steps): plain cells, two per thread",
                      "bytes_per_cell": BYTES["f16"], "cells_per_step": n_plain,
                      "ms_per_step": round(plain_s * 1e3, 4),
+                     # the reference's own bench page also counts a 4-byte flag per cell
+                     # (src/app/bench-page.ts:44-45): 80 bytes for 16-bit storage
+                     "frac_reference_convention": round(achieved * 80.0 / BYTES["f16"] / peak, 4),
                      "traffic": traffic.get("bytes_per_step") if traffic else None,
                      "traffic_source": traffic.get("source") if traffic else None},
         "step_roofline": {"achieved": round(step_achieved, 1), "frac": round(step_achieved / peak, 4),
