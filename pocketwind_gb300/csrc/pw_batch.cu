@@ -42,16 +42,6 @@ struct BatchSeg {
 constexpr int kBatchThreads = pwbatch::NTHREADS;  // 128
 constexpr int kChunk = 50;                        // steps per captured graph
 
-__device__ __forceinline__ uint32_t seg_of(const BatchSeg *segs, uint32_t nsegs, uint32_t w) {
-  uint32_t lo = 0, hi = nsegs - 1;
-  while (lo < hi) {
-    const uint32_t mid = (lo + hi + 1) / 2;
-    if (segs[mid].first <= w) lo = mid;
-    else hi = mid - 1;
-  }
-  return lo;
-}
-
 // PLAIN: the plain items (PAIRS: through the 32-bit cell-pair kernel, which
 // needs 16-bit storage and every member's nx even); otherwise
 // the seam and edge items.
@@ -59,7 +49,7 @@ __device__ __forceinline__ uint32_t seg_of(const BatchSeg *segs, uint32_t nsegs,
 // offset tables sit in shared memory and are reloaded rather than kept live.
 template <int ST, int OP, bool LES, bool ODD, bool PLAIN, bool PAIRS>
 __global__ void __launch_bounds__(kBatchThreads, PLAIN ? 6 : 1) batch_step(const StepParams *params, const BatchSeg *segs,
-                                                             uint32_t nsegs, uint32_t total,
+                                                             const uint32_t *item_seg, uint32_t total,
                                                              const uint32_t *const *lists, const uint32_t *counts,
                                                              uint32_t rows) {
   __shared__ StepParams sp;
@@ -67,7 +57,7 @@ __global__ void __launch_bounds__(kBatchThreads, PLAIN ? 6 : 1) batch_step(const
   const uint32_t tid = threadIdx.x;
   for (uint32_t w = blockIdx.x; w < total; w += gridDim.x) {
     __syncthreads();  // the previous item is done with sp
-    if (tid == 0) cur = segs[seg_of(segs, nsegs, w)];
+    if (tid == 0) cur = segs[__ldg(&item_seg[w])];
     __syncthreads();
     const uint32_t m = cur.member, local = w - cur.first, kind = cur.kind;
     {
@@ -104,10 +94,10 @@ __global__ void __launch_bounds__(kBatchThreads, PLAIN ? 6 : 1) batch_step(const
 
 template <int ST, int OP, bool LES>
 void launch3(bool odd, bool plain, bool pairs, unsigned blocks, cudaStream_t s, const StepParams *params,
-             const BatchSeg *segs, uint32_t nsegs, uint32_t total, const uint32_t *const *lists,
+             const BatchSeg *segs, const uint32_t *item_seg, uint32_t total, const uint32_t *const *lists,
              const uint32_t *counts, uint32_t rows) {
 #define PW_BATCH_LAUNCH(O, P, Q) \
-  batch_step<ST, OP, LES, O, P, Q><<<blocks, kBatchThreads, 0, s>>>(params, segs, nsegs, total, lists, counts, rows)
+  batch_step<ST, OP, LES, O, P, Q><<<blocks, kBatchThreads, 0, s>>>(params, segs, item_seg, total, lists, counts, rows)
   if (plain) {
     if (pairs && ST != pw::STORE_F32) {
       if (odd) PW_BATCH_LAUNCH(true, true, true);
@@ -125,14 +115,14 @@ void launch3(bool odd, bool plain, bool pairs, unsigned blocks, cudaStream_t s, 
 
 template <int ST>
 void launch2(int op, int les, bool odd, bool plain, bool pairs, unsigned blocks, cudaStream_t s,
-             const StepParams *params, const BatchSeg *segs, uint32_t nsegs, uint32_t total,
+             const StepParams *params, const BatchSeg *segs, const uint32_t *item_seg, uint32_t total,
              const uint32_t *const *lists, const uint32_t *counts, uint32_t rows) {
   if (op == pw::OP_REG) {
-    if (les) launch3<ST, pw::OP_REG, true>(odd, plain, pairs, blocks, s, params, segs, nsegs, total, lists, counts, rows);
-    else launch3<ST, pw::OP_REG, false>(odd, plain, pairs, blocks, s, params, segs, nsegs, total, lists, counts, rows);
+    if (les) launch3<ST, pw::OP_REG, true>(odd, plain, pairs, blocks, s, params, segs, item_seg, total, lists, counts, rows);
+    else launch3<ST, pw::OP_REG, false>(odd, plain, pairs, blocks, s, params, segs, item_seg, total, lists, counts, rows);
   } else {
-    if (les) launch3<ST, pw::OP_TRT, true>(odd, plain, pairs, blocks, s, params, segs, nsegs, total, lists, counts, rows);
-    else launch3<ST, pw::OP_TRT, false>(odd, plain, pairs, blocks, s, params, segs, nsegs, total, lists, counts, rows);
+    if (les) launch3<ST, pw::OP_TRT, true>(odd, plain, pairs, blocks, s, params, segs, item_seg, total, lists, counts, rows);
+    else launch3<ST, pw::OP_TRT, false>(odd, plain, pairs, blocks, s, params, segs, item_seg, total, lists, counts, rows);
   }
 }
 
@@ -148,7 +138,10 @@ struct pw_batch {
   // edge items] work segments
   StepParams *params[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   BatchSeg *segs[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-  uint32_t nsegs[2][2] = {{0, 0}, {0, 0}}, total[2][2] = {{0, 0}, {0, 0}};
+  // the segment of every work item, so a block finds its item's member with
+  // one load instead of a search over the segments
+  uint32_t *item_seg[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  uint32_t total[2][2] = {{0, 0}, {0, 0}};
   cudaStream_t side = nullptr;    // the seam and edge items, beside the plain items
   cudaEvent_t fork = nullptr, join = nullptr;
   unsigned sms = 1;               // multiprocessors of the device
@@ -196,7 +189,13 @@ int build_segments(pw_batch *b) {
       PW_TRY(cudaMalloc(&b->segs[par][list], segs[list].size() * sizeof(BatchSeg)));
       PW_TRY(cudaMemcpy(b->segs[par][list], segs[list].data(), segs[list].size() * sizeof(BatchSeg),
                         cudaMemcpyHostToDevice));
-      b->nsegs[par][list] = (uint32_t)segs[list].size();
+      std::vector<uint32_t> table(std::max<uint32_t>(1u, first[list]), 0u);
+      for (uint32_t k = 0; k < segs[list].size(); k++)
+        for (uint32_t i = 0; i < segs[list][k].count; i++) table[segs[list][k].first + i] = k;
+      cudaFree(b->item_seg[par][list]);
+      b->item_seg[par][list] = nullptr;
+      PW_TRY(cudaMalloc(&b->item_seg[par][list], table.size() * sizeof(uint32_t)));
+      PW_TRY(cudaMemcpy(b->item_seg[par][list], table.data(), table.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
       b->total[par][list] = first[list];
     }
   }
@@ -222,18 +221,19 @@ void launch_items(pw_batch *b, bool odd, int macro, bool plain, unsigned blocks,
   const int par = odd ? 1 : 0, list = plain ? 0 : 1;
   const StepParams *params = b->params[par][macro];
   const BatchSeg *segs = b->segs[par][list];
-  const uint32_t nsegs = b->nsegs[par][list], total = b->total[par][list];
+  const uint32_t *item_seg = b->item_seg[par][list];
+  const uint32_t total = b->total[par][list];
   switch (b->storage) {
     case pw::STORE_F16:
-      launch2<pw::STORE_F16>(b->op, b->les, odd, plain, b->pairs, blocks, s, params, segs, nsegs, total, b->lists,
+      launch2<pw::STORE_F16>(b->op, b->les, odd, plain, b->pairs, blocks, s, params, segs, item_seg, total, b->lists,
                              b->counts, b->rows);
       break;
     case pw::STORE_BF16:
-      launch2<pw::STORE_BF16>(b->op, b->les, odd, plain, b->pairs, blocks, s, params, segs, nsegs, total, b->lists,
+      launch2<pw::STORE_BF16>(b->op, b->les, odd, plain, b->pairs, blocks, s, params, segs, item_seg, total, b->lists,
                               b->counts, b->rows);
       break;
     default:
-      launch2<pw::STORE_F32>(b->op, b->les, odd, plain, b->pairs, blocks, s, params, segs, nsegs, total, b->lists,
+      launch2<pw::STORE_F32>(b->op, b->les, odd, plain, b->pairs, blocks, s, params, segs, item_seg, total, b->lists,
                              b->counts, b->rows);
       break;
   }
@@ -400,7 +400,10 @@ void pw_batch_destroy(pw_batch *b) {
   drop_graphs(b);
   for (int par = 0; par < 2; par++) {
     for (int macro = 0; macro < 2; macro++) cudaFree(b->params[par][macro]);
-    for (int list = 0; list < 2; list++) cudaFree(b->segs[par][list]);
+    for (int list = 0; list < 2; list++) {
+      cudaFree(b->segs[par][list]);
+      cudaFree(b->item_seg[par][list]);
+    }
   }
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->join) cudaEventDestroy(b->join);
