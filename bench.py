@@ -238,9 +238,12 @@ def accuracy_leg(steps, threads):
     out = {}
     c = cases.sphere_case("free-slip")
     grid = c.grid()
+    t0 = time.perf_counter()
     s = GpuSolver.create(c.layout, grid, c.params("f32"))
     fx, fy, fz = cases.mean_drag(cases.run_drag(s, c.steps), c.steps, c.average_steps)
     s.destroy()
+    gpu_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
     cpu = O.Cpu64(c.layout, c.tau0, flags=grid.flags, equilibrium_state=(1.0, (c.u_in, 0.0, 0.0)),
                   threads=threads, lateral=c.lateral)
     window = []
@@ -248,12 +251,15 @@ def accuracy_leg(steps, threads):
         cpu.step(8)
         if k > c.steps - c.average_steps:
             window.append(cpu.momentum_exchange()[0])
+    cpu_s = time.perf_counter() - t0
     rfx = float(np.mean(window))
     out["sphere_re100"] = {"grid": "96x48x48", "storage": "f32", "operator": "trt", "lateral": "free-slip",
                            "steps": c.steps, "average_steps": c.average_steps, "fx": fx, "fx_fp64": rfx,
                            "drag_rel_err": abs(fx - rfx) / abs(rfx),
                            "cd": fx * forces.cd_per_lattice_force(grid.frontal_cells),
-                           "frontal_cells": grid.frontal_cells}
+                           "frontal_cells": grid.frontal_cells,
+                           # wall clock of the whole case, a force readback every 8 steps on both sides
+                           "seconds": {"gpu": round(gpu_s, 3), "cpu_fp64": round(cpu_s, 3), "cpu_threads": threads}}
     # the same sphere with interpolated walls on measured link fractions (periodic
     # lateral faces), and halfway walls on that grid for comparison
     c = cases.sphere_case("periodic", walls="bouzidi")
@@ -714,9 +720,12 @@ def main():
     if world == 1 and args.cpu_steps > 0:
         flags = grid.flags.copy()
         cmlups, cdt = cpu_baseline(flags, args.cpu_steps, os.cpu_count() or 1)
+        one, one_dt = cpu_baseline(flags, 1, 1)  # the reference's CPU path is single-threaded JavaScript
         line["cpu_baseline"] = {"value": round(cmlups, 3), "unit": "MLUPS", "cores": os.cpu_count(), "kind": "port",
                                 "sample": f"{args.cpu_steps} full-domain steps of the binary64 CpuSolver "
-                                          f"restatement ({cdt:.1f} s)"}
+                                          f"restatement ({cdt:.1f} s)",
+                                "single_thread": {"value": round(one, 3), "cores": 1,
+                                                  "sample": f"1 full-domain step ({one_dt:.1f} s)"}}
     print(json.dumps(line))
 
 
