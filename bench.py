@@ -27,6 +27,7 @@ cpu_baseline: the binary64 restatement of the reference's CpuSolver (the
           host cores, over a bounded number of full-domain steps.
 accuracy: drag and field errors against that binary64 restatement: the sphere
           at Re 100 (96x48x48, FP32) and the 128x64x64 vehicle in each storage.
+voxelizer: the reference's 200k-triangle voxelizer benchmark at 256x128x128;
 tracers:  the 128x64x64 vehicle in frames of 8 steps with 3-D streaklines, the
           plate smoke and particles advanced after each frame; device times;
 grid_check: the reference's three-tier grid check (GCI band) run one tier
@@ -489,6 +490,38 @@ def grid_check_leg(run_flow_throughs):
             "seconds_one_at_a_time": round(t1 - t0, 3), "seconds_side_by_side": round(t2 - t1, 3)}
 
 
+def voxelizer_leg(iterations=5):
+    """The reference's voxelizer benchmark (tests/unit/voxelize/voxelize.bench.ts):
+    a 200,000-triangle sphere (the fixture's icosphere: 6 subdivisions plus
+    39,360 extra splits, radius 18, centre (84.37, 64.23, 64.41)) voxelized at
+    256 x 128 x 128 without a floor, with a 400 ms budget in the browser.  Wall
+    clock of the whole call on the GPU (mesh upload, three parity-ray
+    projections, wall links, q offsets, boundary list, statistics), best and
+    median of `iterations` after one warm-up, beside the binary64 restatement
+    on one host core; the two grids must be equal."""
+    import numpy as np
+    from oracle import oracle as O
+    from pocketwind_gb300 import meshes
+    from pocketwind_gb300.geometry import voxelize
+    layout = (256, 128, 128)
+    mesh = meshes.icosphere((84.37, 64.23, 64.41), 18, 6, 39360)
+    times = []
+    grid = None
+    for _ in range(iterations + 1):
+        t0 = time.perf_counter()
+        grid = voxelize(mesh, None, layout, False)
+        times.append(time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    ref = O.voxelize(mesh.positions, None, layout, False, link_fractions=False)
+    cpu_s = time.perf_counter() - t0
+    timed = sorted(times[1:])
+    return {"triangles": int(mesh.triangle_count), "grid": "256x128x128", "solid_cells": int(grid.solid_cells),
+            "watertight": bool(grid.watertight), "ms_best": round(1e3 * timed[0], 2),
+            "ms_median": round(1e3 * timed[len(timed) // 2], 2), "reference_budget_ms": 400,
+            "cpu_binary64_one_core_ms": round(1e3 * cpu_s, 1),
+            "equal_to_binary64_restatement": bool(np.array_equal(grid.geometry, ref.geometry))}
+
+
 def tracer_leg(steps):
     """The tracers on the 128x64x64 vehicle (FP32, REG + LES, floor on), stepped
     in frames of 8 steps as the reference's frame loop does (src/app/run.ts:42,
@@ -605,6 +638,8 @@ def main():
     ap.add_argument("--closure-steps", type=int, default=20480,
                     help="fine-grid steps of the learned-closure leg (0 skips the leg)")
     ap.add_argument("--closure-train-steps", type=int, default=20000, help="Adam steps of the closure leg")
+    ap.add_argument("--voxelizer-iterations", type=int, default=5,
+                    help="timed calls of the 200k-triangle voxelizer leg (0 skips the leg)")
     ap.add_argument("--tracer-steps", type=int, default=20000,
                     help="solver steps of the tracer leg, 8 per frame (0 skips the leg)")
     ap.add_argument("--grid-check-flow-throughs", type=float, default=4,
@@ -711,6 +746,8 @@ def main():
         line["batched_tunnels"] = batch_leg(args.batch_steps, peak=peak)
     if world == 1 and args.closure_steps > 0:
         line["learned_closure"] = closure_leg(args.closure_steps, args.closure_train_steps, os.cpu_count() or 1)
+    if world == 1 and args.voxelizer_iterations > 0:
+        line["voxelizer"] = voxelizer_leg(args.voxelizer_iterations)
     if world == 1 and args.tracer_steps > 0:
         line["tracers"] = tracer_leg(args.tracer_steps)
     if world == 1 and args.grid_check_flow_throughs > 0:

@@ -48,6 +48,27 @@ int cuda_status(cudaError_t e, const char *what) {
   return PW_ERR_CUDA;
 }
 
+// Temporaries of one voxelization come from the stream-ordered pool: freeing
+// one never waits for the whole device, and the pool keeps up to 256 MB mapped
+// between calls.
+static cudaError_t tmp_alloc(void *p, size_t bytes, cudaStream_t s) {
+  static bool pool_set = false;
+  if (!pool_set) {
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = 256ull << 20;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
+    pool_set = true;
+  }
+  return cudaMallocAsync(reinterpret_cast<void **>(p), bytes, s);
+}
+static void tmp_free(void *p, cudaStream_t s) {
+  if (p) cudaFreeAsync(p, s);
+}
+
 Grid::~Grid() {
   cudaFree(flags);
   cudaFree(qoff);
@@ -94,9 +115,9 @@ static int exclusive_scan(const uint32_t *in, uint32_t *out, size_t n, uint64_t 
   if (n == 0) { *total = 0; return PW_OK; }
   size_t blocks = (n + 4095) / 4096;
   uint32_t *sums = nullptr, *offs = nullptr;
-  PW_TRY(cudaMalloc(&sums, (blocks + 1) * sizeof(uint32_t)));
-  cudaError_t e = cudaMalloc(&offs, (blocks + 1) * sizeof(uint32_t));
-  if (e != cudaSuccess) { cudaFree(sums); return cuda_status(e, "scan"); }
+  PW_TRY(tmp_alloc(&sums, (blocks + 1) * sizeof(uint32_t), s));
+  cudaError_t e = tmp_alloc(&offs, (blocks + 1) * sizeof(uint32_t), s);
+  if (e != cudaSuccess) { tmp_free(sums, s); return cuda_status(e, "scan"); }
   scan_blocks<<<(unsigned)blocks, 1024, 0, s>>>(in, out, sums, n);
   int rc = PW_OK;
   if (blocks > 1) {
@@ -112,8 +133,8 @@ static int exclusive_scan(const uint32_t *in, uint32_t *out, size_t n, uint64_t 
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) rc = cuda_status(e, "scan total");
   }
-  cudaFree(sums);
-  cudaFree(offs);
+  tmp_free(sums, s);
+  tmp_free(offs, s);
   *total = (uint64_t)last_out + last_in;
   return rc;
 }
@@ -278,9 +299,9 @@ static int vote_mesh(const float *d_mesh, uint32_t ntri, uint32_t nx, uint32_t n
   const int PROJS[3][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}};
   uint8_t *votes = nullptr;
   uint32_t *closed = nullptr;
-  PW_TRY(cudaMalloc(&votes, cells));
-  cudaError_t e = cudaMalloc(&closed, 4);
-  if (e != cudaSuccess) { cudaFree(votes); return cuda_status(e, "voxelize"); }
+  PW_TRY(tmp_alloc(&votes, cells, s));
+  cudaError_t e = tmp_alloc(&closed, 4, s);
+  if (e != cudaSuccess) { tmp_free(votes, s); return cuda_status(e, "voxelize"); }
   int rc = PW_OK;
   uint32_t one = 1u;
   cudaMemsetAsync(votes, 0, cells, s);
@@ -294,9 +315,9 @@ static int vote_mesh(const float *d_mesh, uint32_t ntri, uint32_t nx, uint32_t n
     uint32_t *count = nullptr, *offset = nullptr, *cursor = nullptr;
     double *hits = nullptr;
     uint64_t total = 0;
-    e = cudaMalloc(&count, ncol * 4);
-    if (e == cudaSuccess) e = cudaMalloc(&offset, ncol * 4);
-    if (e == cudaSuccess) e = cudaMalloc(&cursor, ncol * 4);
+    e = tmp_alloc(&count, ncol * 4, s);
+    if (e == cudaSuccess) e = tmp_alloc(&offset, ncol * 4, s);
+    if (e == cudaSuccess) e = tmp_alloc(&cursor, ncol * 4, s);
     if (e != cudaSuccess) rc = cuda_status(e, "voxelize columns");
     if (rc == PW_OK) {
       cudaMemsetAsync(count, 0, ncol * 4, s);
@@ -305,15 +326,14 @@ static int vote_mesh(const float *d_mesh, uint32_t ntri, uint32_t nx, uint32_t n
       rc = exclusive_scan(count, offset, ncol, &total, s);
     }
     if (rc == PW_OK) {
-      e = cudaMalloc(&hits, (total ? total : 1) * sizeof(double));
+      e = tmp_alloc(&hits, (total ? total : 1) * sizeof(double), s);
       if (e != cudaSuccess) rc = cuda_status(e, "voxelize hits");
     }
     if (rc == PW_OK) {
       raster_kernel<<<ntri, 128, 0, s>>>(d_mesh, P, count, offset, cursor, hits, 1);
       column_kernel<<<nblk(ncol), 256, 0, s>>>(P, count, offset, hits, votes, closed);
     }
-    cudaStreamSynchronize(s);
-    cudaFree(count); cudaFree(offset); cudaFree(cursor); cudaFree(hits);
+    tmp_free(count, s); tmp_free(offset, s); tmp_free(cursor, s); tmp_free(hits, s);
   }
   uint32_t closed_h = 1;
   if (rc == PW_OK) {
@@ -323,8 +343,8 @@ static int vote_mesh(const float *d_mesh, uint32_t ntri, uint32_t nx, uint32_t n
     if (e != cudaSuccess) rc = cuda_status(e, "voxelize vote");
   }
   *watertight = closed_h != 0;
-  cudaFree(votes);
-  cudaFree(closed);
+  tmp_free(votes, s);
+  tmp_free(closed, s);
   return rc;
 }
 
@@ -473,8 +493,8 @@ __global__ void link_fraction_kernel(const uint32_t *flags, const uint32_t *qoff
   if (miss) atomicAdd(missed, miss);
 }
 
-static void free_bins(DevBins &B) {
-  cudaFree(B.bounds); cudaFree(B.start); cudaFree(B.items);
+static void free_bins(DevBins &B, cudaStream_t s) {
+  tmp_free(B.bounds, s); tmp_free(B.start, s); tmp_free(B.items, s);
   B = DevBins();
 }
 
@@ -486,9 +506,9 @@ static int build_bins(const float *d_mesh, uint32_t ntri, uint32_t nx, uint32_t 
   size_t nb = (size_t)B.bx * B.by * B.bz;
   uint32_t *count = nullptr;
   uint64_t total = 0;
-  cudaError_t e = cudaMalloc(&B.bounds, (ntri ? ntri : 1) * 6 * sizeof(float));
-  if (e == cudaSuccess) e = cudaMalloc(&B.start, (nb + 1) * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&count, nb * 4);
+  cudaError_t e = tmp_alloc(&B.bounds, (ntri ? ntri : 1) * 6 * sizeof(float), s);
+  if (e == cudaSuccess) e = tmp_alloc(&B.start, (nb + 1) * 4, s);
+  if (e == cudaSuccess) e = tmp_alloc(&count, nb * 4, s);
   int rc = e == cudaSuccess ? PW_OK : cuda_status(e, "triangle bins");
   if (rc == PW_OK) {
     cudaMemsetAsync(count, 0, nb * 4, s);
@@ -497,7 +517,7 @@ static int build_bins(const float *d_mesh, uint32_t ntri, uint32_t nx, uint32_t 
   }
   if (rc == PW_OK) {
     set_u32_kernel<<<1, 1, 0, s>>>(B.start + nb, (uint32_t)total);
-    e = cudaMalloc(&B.items, (total ? total : 1) * 4);
+    e = tmp_alloc(&B.items, (total ? total : 1) * 4, s);
     if (e != cudaSuccess) rc = cuda_status(e, "triangle bins");
   }
   if (rc == PW_OK) {
@@ -506,8 +526,8 @@ static int build_bins(const float *d_mesh, uint32_t ntri, uint32_t nx, uint32_t 
     e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) rc = cuda_status(e, "triangle bins");
   }
-  cudaFree(count);
-  if (rc != PW_OK) { free_bins(B); return rc; }
+  tmp_free(count, s);
+  if (rc != PW_OK) { free_bins(B, s); return rc; }
   *out = B;
   return PW_OK;
 }
@@ -522,7 +542,7 @@ static int measure_links(pw_grid *g, const float *d_body, uint32_t nbody, const 
   uint32_t *missed = nullptr;
   uint32_t missed_h = 0;
   if (rc == PW_OK) {
-    cudaError_t e = cudaMalloc(&missed, 4);
+    cudaError_t e = tmp_alloc(&missed, 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(missed, 0, 4, s);
     if (e == cudaSuccess) {
       link_fraction_kernel<<<nblk(g->cells, 128), 128, 0, s>>>(g->flags, g->qoff, g->fractions, g->nx, g->ny, g->nz,
@@ -532,9 +552,9 @@ static int measure_links(pw_grid *g, const float *d_body, uint32_t nbody, const 
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) rc = cuda_status(e, "link fractions");
   }
-  cudaFree(missed);
-  free_bins(body);
-  free_bins(sup);
+  tmp_free(missed, s);
+  free_bins(body, s);
+  free_bins(sup, s);
   if (rc == PW_OK) g->stats.missed_links = missed_h;
   return rc;
 }
@@ -551,11 +571,11 @@ static int finish_grid(pw_grid *g, int floor_on, bool body_closed, bool supports
   uint32_t *link_count = nullptr, *is_boundary = nullptr, *scan = nullptr, *solid = nullptr;
   uint8_t *proj = nullptr;
   size_t plane = (size_t)g->ny * g->nz;
-  cudaError_t e = cudaMalloc(&link_count, cells * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&is_boundary, cells * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&scan, cells * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&solid, 16);
-  if (e == cudaSuccess) e = cudaMalloc(&proj, 2 * plane);
+  cudaError_t e = tmp_alloc(&link_count, cells * 4, s);
+  if (e == cudaSuccess) e = tmp_alloc(&is_boundary, cells * 4, s);
+  if (e == cudaSuccess) e = tmp_alloc(&scan, cells * 4, s);
+  if (e == cudaSuccess) e = tmp_alloc(&solid, 16, s);
+  if (e == cudaSuccess) e = tmp_alloc(&proj, 2 * plane, s);
   int rc = e == cudaSuccess ? PW_OK : cuda_status(e, "voxelize counts");
   uint32_t counts[4] = {0, 0, 0, 0};
   if (rc == PW_OK) {
@@ -590,7 +610,7 @@ static int finish_grid(pw_grid *g, int floor_on, bool body_closed, bool supports
       if (e != cudaSuccess) rc = cuda_status(e, "voxelize finish");
     }
   }
-  cudaFree(link_count); cudaFree(is_boundary); cudaFree(scan); cudaFree(solid); cudaFree(proj);
+  tmp_free(link_count, s); tmp_free(is_boundary, s); tmp_free(scan, s); tmp_free(solid, s); tmp_free(proj, s);
   if (rc != PW_OK) return rc;
   pw_grid_stats &st = g->stats;
   st.nx = g->nx; st.ny = g->ny; st.nz = g->nz;
@@ -679,8 +699,8 @@ int pw_voxelize_opts(const float *body, uint32_t body_triangles, const float *su
   bool body_closed = true, sup_closed = true;
   cudaError_t e = cudaMalloc(&g->flags, cells * 4);
   float *d_sup = nullptr;
-  if (e == cudaSuccess) e = cudaMalloc(&d_mesh, (body_triangles ? body_triangles : 1) * 36);
-  if (e == cudaSuccess) e = cudaMalloc(&d_sup, (support_triangles ? support_triangles : 1) * 36);
+  if (e == cudaSuccess) e = tmp_alloc(&d_mesh, (body_triangles ? body_triangles : 1) * 36, s);
+  if (e == cudaSuccess) e = tmp_alloc(&d_sup, (support_triangles ? support_triangles : 1) * 36, s);
   if (e != cudaSuccess) rc = cuda_status(e, "pw_voxelize");
   if (rc == PW_OK) {
     cudaMemsetAsync(g->flags, 0, cells * 4, s);
@@ -697,9 +717,9 @@ int pw_voxelize_opts(const float *body, uint32_t body_triangles, const float *su
   }
   if (rc == PW_OK && link_fractions && g->nfrac)
     rc = measure_links(g, d_mesh, body_triangles, d_sup, support_triangles, supports != nullptr, floor_on, s);
+  tmp_free(d_mesh, s);
+  tmp_free(d_sup, s);
   cudaStreamSynchronize(s);
-  cudaFree(d_mesh);
-  cudaFree(d_sup);
   cudaStreamDestroy(s);
   if (rc != PW_OK) { delete g; return rc; }
   *out = g;
