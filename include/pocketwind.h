@@ -122,7 +122,10 @@ PW_API int pw_device_count(void);
  * EQ/FLOOR boundaries, pull-direction wall masks, q offsets with halfway
  * fractions, and the ascending body boundary list.  Meshes are float32
  * triangle soups (9 floats per triangle) in lattice cells; supports may be
- * NULL.  Returns PW_ERR_INVALID for dims below 2 or non-finite coordinates. */
+ * NULL.  Returns PW_ERR_INVALID for dims below 2 or non-finite coordinates.
+ * The call's temporaries come from the device's default stream-ordered memory
+ * pool; the first call raises that pool's release threshold to 256 MB for the
+ * process, so later calls reuse the mapped memory. */
 PW_API int pw_voxelize(const float *body, uint32_t body_triangles, const float *supports,
                 uint32_t support_triangles, uint32_t nx, uint32_t ny, uint32_t nz,
                 int floor_on, pw_grid **out);
