@@ -122,23 +122,30 @@ class ClockSampler:
             self.proc.kill()
         self.file.flush()
         self.file.seek(0)
-        rows = [r.split(",") for r in self.file.read().strip().splitlines() if r.strip()]
+        text = self.file.read()
         os.unlink(self.file.name)
-        sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in rows:
-            try:
-                sm.append(float(r[1]))
-                mx.append(float(r[2]))
-                for k, name in enumerate(names):
-                    if r[5 + k].strip().lower().startswith("active"):
-                        reasons.add(name)
-            except (ValueError, IndexError):
-                continue
-        if sm:
-            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                   "samples": len(sm)}
-        return out
+        return parse_clock_rows(text) or out
+
+
+def parse_clock_rows(text):
+    """Median SM clock, the highest maximum clock and the throttle reasons seen
+    in `nvidia-smi --query-gpu=<ClockSampler.FIELDS> --format=csv,noheader,nounits`
+    output; None when no row parses."""
+    sm, mx, reasons = [], [], set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in text.strip().splitlines():
+        r = line.split(",")
+        try:
+            sm.append(float(r[1]))
+            mx.append(float(r[2]))
+            for k, name in enumerate(names):
+                if r[5 + k].strip().lower().startswith("active"):
+                    reasons.add(name)
+        except (ValueError, IndexError):
+            continue
+    if not sm:
+        return None
+    return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
 
 
 def barrier(world):

@@ -1,6 +1,7 @@
-"""The benchmark's replica path on two CPU ranks (gloo): the barrier, the
-max-over-ranks timing and the whole-job aggregate that `bench.py --gpus N`
-reports when torchrun starts one replica per GPU."""
+"""The benchmark's host logic on the CPU: the replica path on two gloo ranks
+(the barrier, the max-over-ranks timing and the whole-job aggregate that
+`bench.py --gpus N` reports when torchrun starts one replica per GPU), and the
+clock record parsed from nvidia-smi samples."""
 import os
 import socket
 
@@ -50,3 +51,21 @@ def test_one_rank_needs_no_process_group():
     bench.barrier(1)
     assert bench.max_over_ranks([2, 5.5], 1) == [2.0, 5.5]
     assert bench.job_mlups(33554432, 100, 1, 50.0) == pytest.approx(67108.864)
+
+
+def test_clock_rows_report_median_clock_and_throttle_reasons():
+    """The clocks record that rejects a throttled run: median SM clock under load,
+    the maximum clock, and every throttle reason that was active in any sample."""
+    import bench
+    text = "\n".join([
+        "0, 2070, 2070, 950.1, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "0, 1980, 2070, 1390.5, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+        "0, 2070, 2070, 1200.0, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "garbage line",
+        "0, 1400, 2070, 1000.0, 0x0000000000000008, Active, Not Active, Not Active, Not Active",
+    ])
+    got = bench.parse_clock_rows(text)
+    assert got == {"sm_mhz": 2025.0, "sm_max_mhz": 2070.0, "reasons": ["hw_slowdown", "sw_power_cap"],
+                   "samples": 4}
+    assert bench.parse_clock_rows("") is None
+    assert bench.parse_clock_rows("not,a,number") is None
