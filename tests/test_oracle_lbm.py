@@ -614,3 +614,28 @@ def test_free_slip_binary32_tracks_binary64():
         d.step()
     a, b = f.populations().astype(np.float64), d.populations
     assert np.abs(a - b).max() / np.abs(b).max() < 1e-5
+
+
+@pytest.mark.parametrize("delta", [2.0 ** -28, -(2.0 ** -28), 2.0 ** -20])
+def test_binary32_path_keeps_tiny_density_deviations(delta):
+    """tests/unit/shader-density.test.ts:48-67: a rest state whose populations
+    are f32(f32(w_i) * delta) keeps its density deviation through the binary32
+    step, because the equilibrium is built from rho_delta (the sum of the
+    shifted populations), not from rho - 1: rho is f32(1 + delta), and the next
+    state's populations sum back to delta within 2e-6 relative."""
+    layout = (2, 2, 2)
+    cells = 8
+    geometry = np.concatenate([np.zeros(cells, np.uint32), np.full(cells, NO_Q, np.uint32)])
+    s = O.Wgsl32(*layout, 0.8, 0.0, geometry)
+    for n in range(cells):
+        for i in range(19):
+            s.poke(i, n, np.float32(np.float32(W[i]) * np.float32(delta)))
+    s.step(0.0, True)
+    rho = s.macros().reshape(-1, 4)[:, 0]
+    assert np.all(rho == np.float32(1.0 + np.float32(delta)))
+    g = s.populations().reshape(19, cells)
+    for n in range(cells):
+        recovered = np.float32(0.0)
+        for i in range(19):
+            recovered = np.float32(recovered + g[i, n])
+        assert abs(float(recovered) / delta - 1.0) < 2e-6
