@@ -156,6 +156,14 @@ PW_API void pw_grid_destroy(pw_grid *grid);
 
 /* ---------------------------------------------------------------- solver */
 
+/* The checks of GpuSolver.create that need no device: packSolverParams
+ * (src/lbm/gpu-solver.ts:80-116) throws RangeError before any device work
+ * for a grid dimension below 1, a relaxation time that is not above 1/2 after
+ * binary32 rounding (0.5 + 2^-26 is not; 0.5 + 2^-24 is), or an inlet speed
+ * that is not finite in binary32 (1e100 overflows).  Here also an unknown
+ * enumeration or a grid past 2^32 cells.  PW_OK or PW_ERR_INVALID with the
+ * message in pw_last_error(); callable without a GPU. */
+PW_API int pw_validate_desc(const pw_domain_desc *desc);
 /* GpuSolver.create (src/lbm/gpu-solver.ts:158-335): validates the parameters
  * (tau0 > 1/2 after binary32 rounding, finite inlet speed), allocates every
  * buffer or none (PW_ERR_OOM frees partial allocations) and resets to the

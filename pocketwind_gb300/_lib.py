@@ -60,6 +60,7 @@ SIGNATURES = {
     "pw_grid_read_geometry": (_int, [_vp, _vp, _sz]),
     "pw_grid_read_boundary": (_int, [_vp, _vp, _sz]),
     "pw_grid_destroy": (None, [_vp]),
+    "pw_validate_desc": (_int, [C.POINTER(DomainDesc)]),
     "pw_domain_create": (_int, [C.POINTER(DomainDesc), _vp, _PP]),
     "pw_domain_destroy": (None, [_vp]),
     "pw_reset": (_int, [_vp]),

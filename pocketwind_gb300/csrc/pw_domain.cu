@@ -402,15 +402,13 @@ int build_edge_list(pw_domain *d, Allocs &a) {
   return PW_OK;
 }
 
-}  // namespace
-
-extern "C" {
-
-int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain **out) {
-  if (!desc || !grid || !out) { set_error("NULL argument"); return PW_ERR_INVALID; }
-  *out = nullptr;
-  if (desc->nx != grid->nx || desc->ny != grid->ny || desc->nz != grid->nz) {
-    set_error("Geometry must match the solver layout and contain flags and q offsets.");
+// The checks of a domain description that need no device, in the order
+// pw_domain_create applies them: the enumerations, then packSolverParams's
+// (gpu-solver.ts:88-105) relaxation time and inlet speed in binary32, then the
+// size.  Writes the binary32 viscosity and inlet speed when asked.
+int check_desc(const pw_domain_desc *desc, float *nu_out, float *uin_out) {
+  if (desc->nx < 1 || desc->ny < 1 || desc->nz < 1) {
+    set_error("Grid dimensions must be positive safe integers.");
     return PW_ERR_INVALID;
   }
   if (desc->storage < 0 || desc->storage > 2) { set_error("Unknown population storage."); return PW_ERR_INVALID; }
@@ -438,10 +436,35 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
     set_error("Relaxation time must exceed 0.5 and inlet speed must be finite.");
     return PW_ERR_INVALID;
   }
-  size_t cells = grid->cells;
+  const size_t cells = (size_t)desc->nx * desc->ny * desc->nz;
   // cell indices and the plane stride (cells rounded up to 64) stay 32-bit;
   // element indices into the population array are 64-bit
   if (cells > 0xffffffffull - 64) { set_error("The grid exceeds 2^32 cells."); return PW_ERR_INVALID; }
+  if (nu_out) *nu_out = nu;
+  if (uin_out) *uin_out = uin;
+  return PW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pw_validate_desc(const pw_domain_desc *desc) {
+  if (!desc) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  return check_desc(desc, nullptr, nullptr);
+}
+
+int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain **out) {
+  if (!desc || !grid || !out) { set_error("NULL argument"); return PW_ERR_INVALID; }
+  *out = nullptr;
+  if (desc->nx != grid->nx || desc->ny != grid->ny || desc->nz != grid->nz) {
+    set_error("Geometry must match the solver layout and contain flags and q offsets.");
+    return PW_ERR_INVALID;
+  }
+  float nu = 0.0f, uin = 0.0f;
+  const int checked = check_desc(desc, &nu, &uin);
+  if (checked != PW_OK) return checked;
+  size_t cells = grid->cells;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); set_error("No CUDA device is available."); return PW_ERR_CUDA; }
 

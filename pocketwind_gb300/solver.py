@@ -64,7 +64,14 @@ class GpuSolver:
 
     # -------------------------------------------------------------- create
     @staticmethod
-    def create(layout, grid: VoxelGrid, params: SolverParams) -> Union["GpuSolver", AllocationFailure]:
+    def validate(layout, params: SolverParams) -> None:
+        """Raise RangeError for parameters that GpuSolver.create would refuse
+        before any device work (packSolverParams, gpu-solver.ts:80-116); needs
+        the library but no GPU."""
+        GpuSolver._desc(layout, params)
+
+    @staticmethod
+    def _desc(layout, params: SolverParams):
         ramp = params.ramp_steps
         if not isinstance(ramp, int) or ramp < 0:
             raise RangeError("Ramp steps must be a non-negative safe integer.")
@@ -72,15 +79,26 @@ class GpuSolver:
             raise RangeError("Unknown operator, wall treatment or precision.")
         if params.lateral not in ("periodic", "free-slip") or params.kernel not in ("auto", "cell", "tile"):
             raise RangeError("Unknown lateral boundary or kernel choice.")
-        nx, ny, nz = (int(v) for v in layout)
+        dims = []
+        for v in layout:
+            if isinstance(v, bool) or not float(v).is_integer() or not 1 <= v < 2 ** 32:
+                raise RangeError("Grid dimensions must be positive safe integers.")
+            dims.append(int(v))
+        d = _lib.DomainDesc(*dims, float(params.tau0), float(params.u_in), int(bool(params.les)),
+                            OPERATORS[params.operator], WALLS[params.walls], PRECISIONS[params.precision],
+                            ramp, int(bool(params.strict)), {"auto": 0, "cell": 1, "tile": 2}[params.kernel],
+                            {"periodic": 0, "free-slip": 1}[params.lateral])
+        _lib.check(_lib.load().pw_validate_desc(C.byref(d)), "GpuSolver.create")
+        return d
+
+    @staticmethod
+    def create(layout, grid: VoxelGrid, params: SolverParams) -> Union["GpuSolver", AllocationFailure]:
+        d = GpuSolver._desc(layout, params)
+        nx, ny, nz = d.nx, d.ny, d.nz
         if (nx, ny, nz) != (grid.nx, grid.ny, grid.nz):
             raise RangeError("Geometry must match the solver layout and contain flags and q offsets.")
         L = _lib.load()
         _lib.require_gpu()
-        d = _lib.DomainDesc(nx, ny, nz, float(params.tau0), float(params.u_in), int(bool(params.les)),
-                            OPERATORS[params.operator], WALLS[params.walls], PRECISIONS[params.precision],
-                            ramp, int(bool(params.strict)), {"auto": 0, "cell": 1, "tile": 2}[params.kernel],
-                            {"periodic": 0, "free-slip": 1}[params.lateral])
         out = C.c_void_p()
         rc = L.pw_domain_create(C.byref(d), grid._handle.ptr, C.byref(out))
         if rc == _lib.PW_ERR_OOM:
