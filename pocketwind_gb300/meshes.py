@@ -8,8 +8,10 @@ voxelizer and the CPU checker:
   100 mm nose radius and 25 degree slant, stilts, 100 mm cube, lat-long sphere);
 * ``icosphere`` follows the test fixture generator
   tests/unit/voxelize/fixtures.ts:48-108 (icosahedron, midpoint subdivision);
-* ``place_mesh`` follows src/geometry/transform.ts:118-143 (scale by the longest
-  extent, nose at nx/4, centred y, z centred or on the floor wall at z = 0.5).
+* ``place_mesh``, ``default_orientation`` and ``default_length_cells`` follow
+  src/geometry/transform.ts:31-143 (flow and up axes rotated onto +x and +z,
+  scale by the longest extent, nose at nx/4, centred lateral axis, z centred or
+  on the floor wall at z = 0.5; the dropped-mesh defaults).
 
 Meshes are ``Mesh(positions: float32[9*T], triangle_count)`` in lattice cells.
 Coordinates are computed in binary64 and stored in binary32, as the reference's
@@ -22,6 +24,8 @@ from dataclasses import dataclass
 from typing import Optional, Sequence
 
 import numpy as np
+
+from ._lib import RangeError
 
 
 @dataclass
@@ -195,35 +199,100 @@ def icosphere(centre, radius: float, subdivisions: int = 5, extra_splits: int = 
 
 
 # --------------------------------------------------------------- placement
-def place_mesh(mesh: Mesh, nx: int, ny: int, nz: int, length_cells: float, floor: bool,
-               supports: Optional[Mesh] = None):
-    """transform.ts:118-143 with flow along +x and z up."""
-    for size in (nx, ny, nz):
-        if int(size) != size or size < 2:
-            raise ValueError("Grid dimensions must be integers of at least two cells.")
-    if not (math.isfinite(length_cells) and length_cells > 0):
-        raise ValueError("Body length in cells must be finite and positive.")
-    if mesh.triangle_count < 1:
-        raise ValueError("Mesh positions must match a positive triangle count.")
+# Placement and blockage limits of the tunnel (transform.ts:14-19).
+NOSE_FRACTION_NX = 0.25
+LENGTH_CAP_NX = 0.4
+BLOCKAGE_MAX = 0.08
+FLOOR_WALL_Z_CELLS = 0.5
+_AXES = "xyz"
+
+
+def _mesh_bounds(mesh: Mesh):
+    """meshBounds (transform.ts:31-49): binary64 bounds of the float32 vertices."""
+    if mesh.triangle_count < 1 or mesh.positions.size != 9 * mesh.triangle_count:
+        raise RangeError("Mesh positions must match a positive triangle count.")
     p = mesh.positions.reshape(-1, 3).astype(np.float64)
-    lo, hi = p.min(axis=0), p.max(axis=0)
-    longest = float((hi - lo).max())
+    if not np.isfinite(p).all():
+        raise RangeError("Mesh coordinates must be finite.")
+    return p.min(axis=0), p.max(axis=0)
+
+
+def _longest(extents) -> float:
+    longest = float(max(extents))
     if longest == 0:
-        raise ValueError("Mesh must have a nonzero extent.")
-    scale = length_cells / longest
-    nose = lo[0]
-    centre_y = (lo[1] + hi[1]) / 2
-    centre_z = (lo[2] + hi[2]) / 2
-    lowest = lo[2]
-    if supports is not None:
-        lowest = min(lowest, float(supports.positions.reshape(-1, 3)[:, 2].min()))
+        raise RangeError("Mesh must have a nonzero extent.")
+    return longest
+
+
+def _check_layout(nx, ny, nz) -> None:
+    for size in (nx, ny, nz):
+        if isinstance(size, bool) or not float(size).is_integer() or size < 2 or size > 2 ** 53:
+            raise RangeError("Grid dimensions must be integers of at least two cells.")
+
+
+def default_orientation(mesh: Mesh):
+    """defaultOrientation (transform.ts:70-74): z up, positive flow along the
+    longer horizontal extent (x on ties).  Returns (flow_axis, flow_sign, up_axis)."""
+    lo, hi = _mesh_bounds(mesh)
+    ext = hi - lo
+    return ("y" if ext[1] > ext[0] else "x"), 1, "z"
+
+
+def default_length_cells(mesh: Mesh, nx: int, ny: int, nz: int, floor: bool) -> float:
+    """defaultLengthCells (transform.ts:77-87): the body length in cells for a
+    dropped mesh, capped at 0.4 nx and by an 8% blockage of its default
+    orientation's frontal bounding box (rounded down to whole cells)."""
+    del floor  # the reference takes it and does not use it
+    _check_layout(nx, ny, nz)
+    lo, hi = _mesh_bounds(mesh)
+    ext = hi - lo
+    longest = _longest(ext)
+    frontal = min(ext[0], ext[1]) * ext[2]
+    blockage = math.inf if frontal == 0 else math.floor(longest * math.sqrt(BLOCKAGE_MAX * ny * nz / frontal))
+    return min(LENGTH_CAP_NX * nx, blockage)
+
+
+def _lateral_axis(flow_axis: str, flow_sign: int, up_axis: str):
+    """lateralAxis (transform.ts:89-100): the third axis, signed so that
+    y = up x flow keeps every orientation right-handed."""
+    if flow_axis not in _AXES or up_axis not in _AXES or flow_sign not in (1, -1):
+        raise RangeError("Flow and up must be coordinate axes.")
+    if flow_axis == up_axis:
+        raise RangeError("Flow and up axes must differ.")
+    axis = next(a for a in _AXES if a not in (flow_axis, up_axis))
+    positive = (up_axis, flow_axis) in (("z", "x"), ("x", "y"), ("y", "z"))
+    return _AXES.index(axis), (flow_sign if positive else -flow_sign)
+
+
+def place_mesh(mesh: Mesh, nx: int, ny: int, nz: int, length_cells: float, floor: bool,
+               supports: Optional[Mesh] = None, flow_axis: str = "x", flow_sign: int = 1, up_axis: str = "z"):
+    """placeMesh (transform.ts:115-143): rotate flow_axis (sign flow_sign) onto
+    lattice +x and up_axis onto +z, scale body and supports together so the
+    body's longest extent spans length_cells, put the nose at nx / 4, centre
+    the lateral axis, and centre z or rest the union of body and supports on
+    the floor wall at z = 1/2.  Returns (body, supports or None)."""
+    _check_layout(nx, ny, nz)
+    if not (math.isfinite(length_cells) and length_cells > 0):
+        raise RangeError("Body length in cells must be finite and positive.")
+    lat, lat_sign = _lateral_axis(flow_axis, flow_sign, up_axis)
+    fa, ua = _AXES.index(flow_axis), _AXES.index(up_axis)
+    lo, hi = _mesh_bounds(mesh)
+    sup_lo = _mesh_bounds(supports)[0] if supports is not None else None
+    scale = length_cells / _longest(hi - lo)
+    nose = lo[fa] if flow_sign == 1 else hi[fa]
+    centre_y = (lo[lat] + hi[lat]) / 2
+    centre_z = (lo[ua] + hi[ua]) / 2
+    lowest = min(lo[ua], sup_lo[ua]) if sup_lo is not None else lo[ua]
 
     def tf(m: Mesh) -> Mesh:
         q = m.positions.reshape(-1, 3).astype(np.float64)
         out = np.empty_like(q)
-        out[:, 0] = 0.25 * nx + (q[:, 0] - nose) * scale
-        out[:, 1] = ny / 2 + (q[:, 1] - centre_y) * scale
-        out[:, 2] = (0.5 + (q[:, 2] - lowest) * scale) if floor else (nz / 2 + (q[:, 2] - centre_z) * scale)
+        out[:, 0] = NOSE_FRACTION_NX * nx + flow_sign * (q[:, fa] - nose) * scale
+        out[:, 1] = ny / 2 + lat_sign * (q[:, lat] - centre_y) * scale
+        if floor:
+            out[:, 2] = FLOOR_WALL_Z_CELLS + (q[:, ua] - lowest) * scale
+        else:
+            out[:, 2] = nz / 2 + (q[:, ua] - centre_z) * scale
         return Mesh(out.astype(np.float32).reshape(-1), m.triangle_count)
 
     return tf(mesh), (tf(supports) if supports is not None else None)
