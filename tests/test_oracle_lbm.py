@@ -639,3 +639,28 @@ def test_binary32_path_keeps_tiny_density_deviations(delta):
         for i in range(19):
             recovered = np.float32(recovered + g[i, n])
         assert abs(float(recovered) / delta - 1.0) < 2e-6
+
+
+def test_lattice_tables():
+    """tests/unit/lattice/lattice.test.ts: the oracle's D3Q19 table (the order
+    the wall masks use) has 19 distinct velocities paired with their opposites
+    at (2k-1, 2k), rest, axial and diagonal weights that sum to one, zero
+    momentum, and isotropic second and fourth moments."""
+    c, w = O.LATTICE_C.astype(np.float64), O.LATTICE_W
+    assert np.array_equal(c, np.asarray(C, np.float64)) and np.array_equal(w, np.asarray(W))
+    assert len({tuple(v) for v in c}) == 19
+    for i in range(19):
+        j = opp(i)
+        assert j == (0 if i == 0 else (i + 1 if i % 2 else i - 1)) and opp(j) == i
+        assert np.array_equal(c[j], -c[i] + 0.0) and w[j] == w[i]
+    assert w[0] == 1 / 3 and np.all(w[1:7] == 1 / 18) and np.all(w[7:] == 1 / 36)
+    assert abs(w.sum() - 1) < 1e-15
+    for a in range(3):
+        assert abs((w * c[:, a]).sum()) < 1e-15
+        for b in range(3):
+            assert abs((w * c[:, a] * c[:, b]).sum() - (1 / 3 if a == b else 0)) < 1e-15
+            for d in range(3):
+                for e in range(3):
+                    fourth = (w * c[:, a] * c[:, b] * c[:, d] * c[:, e]).sum()
+                    expected = ((a == b and d == e) + (a == d and b == e) + (a == e and b == d)) / 9
+                    assert abs(fourth - expected) < 1e-15

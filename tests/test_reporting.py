@@ -3,6 +3,7 @@ tests/unit/forces/grid-band.test.ts, physical.test.ts, reference-area.test.ts
 and tests/unit/app/grid-check.test.ts (plan, availability, mean, runner order,
 cancel, refusal of a stepped-down grid, wording)."""
 import math
+import sys
 
 import pytest
 
@@ -264,3 +265,52 @@ def test_concurrent_grid_check_equals_one_at_a_time():
     assert [r.length_cells for r in conc.rows] == [16, 24, 32]
     for r in conc.rows:
         assert r.cd is not None and 0.1 < r.cd < 10
+
+
+# ---------------------------------------------------------------- units.test.ts
+def test_units_constants():
+    """tests/unit/units/units.test.ts:11-15."""
+    from pocketwind_gb300 import forces
+    assert R.NU_AIR == 1.5e-5 and forces.U_LU == 0.05 and R.NU_MIN_LU == 1e-2
+
+
+def test_physical_to_lattice_cases():
+    """units.test.ts:17-51: nominal Re from metres, Reynolds similarity under
+    refinement, a direct Re, and the viscosity floor at high Re."""
+    re, nu = R.physical_to_lattice(102.4, speed_mps=40, ref_length_m=1.044)
+    assert re == pytest.approx(2784000, abs=1e-8) and nu == R.NU_MIN_LU
+    coarse = R.physical_to_lattice(20, speed_mps=5, ref_length_m=0.0001)
+    fine = R.physical_to_lattice(40, speed_mps=5, ref_length_m=0.0001)
+    assert fine[0] == coarse[0] and fine[1] == pytest.approx(2 * coarse[1], abs=1e-15)
+    assert R.physical_to_lattice(20, re=100) == (100, 0.01)
+    for re in (500000, 1000000, 1e12):
+        assert R.physical_to_lattice(10, re=re) == (re, R.NU_MIN_LU)
+    re, nu = R.physical_to_lattice(10, speed_mps=60, ref_length_m=1.044)
+    assert re == pytest.approx(4176000, abs=1e-8) and nu == R.NU_MIN_LU
+
+
+@pytest.mark.parametrize("value", [0, -1, math.nan, math.inf])
+def test_physical_to_lattice_rejects_nonpositive_or_nonfinite_inputs(value):
+    """units.test.ts:53-64."""
+    for kwargs in (dict(ref_length_cells=20, re=value), dict(ref_length_cells=value, re=100),
+                   dict(ref_length_cells=20, speed_mps=value, ref_length_m=1),
+                   dict(ref_length_cells=20, speed_mps=40, ref_length_m=value)):
+        with pytest.raises(RangeError):
+            R.physical_to_lattice(**kwargs)
+
+
+def test_physical_to_lattice_rejects_unrepresentable_derived_scales():
+    """units.test.ts:66-73: an overflowing Re and an infinite viscosity."""
+    with pytest.raises(RangeError):
+        R.physical_to_lattice(20, speed_mps=sys.float_info.max, ref_length_m=2)
+    with pytest.raises(RangeError):
+        R.physical_to_lattice(20, re=5e-324)
+
+
+def test_cd_per_lattice_force():
+    """units.test.ts:76-86."""
+    from pocketwind_gb300 import forces
+    force = 0.5 * forces.U_LU * forces.U_LU * 432
+    assert force * forces.cd_per_lattice_force(432) == pytest.approx(1, abs=1e-12)
+    with pytest.raises(RangeError):
+        forces.cd_per_lattice_force(0)
