@@ -143,3 +143,32 @@ def test_gpu_body_matches_host_writer(precision):
     with pytest.raises(RangeError):
         F.solver_vtk(s, 0.004, 0.0)
     s.destroy()
+
+
+def test_field_export_known_file():
+    """tests/unit/io/field-export.test.ts:23-61 on an 8^3 field: the inlet speed
+    maps 0.05 to 20 m/s, the header, the first 100 densities and velocities read
+    back big-endian, the file size, the unchanged source arrays, the refused
+    speeds and the file names."""
+    n, cells = 8, 512
+    rho = (1 + np.arange(cells) / 1024).astype(np.float32)
+    vel = np.tile(np.array([0.05, 0.025, -0.0125], np.float32), cells)
+    source = vel.copy()
+    field = F.lattice_to_field(vel, 20.0)
+    assert list(field[:3]) == [20, 10, -5] and np.array_equal(vel, source)
+    data = F.field_vtk_bytes(n, n, n, 0.004, 20.0, rho, vel)
+    header = ("# vtk DataFile Version 3.0\nPocketWind field\nBINARY\nDATASET STRUCTURED_POINTS\n"
+              "DIMENSIONS 8 8 8\nORIGIN 0 0 0\nSPACING 0.004 0.004 0.004\nPOINT_DATA 512\n"
+              "SCALARS rho float 1\nLOOKUP_TABLE default\n").encode()
+    assert data[:len(header)] == header
+    v0 = len(header) + cells * 4 + 1 + len(b"VECTORS velocity float\n")
+    for cell in range(100):
+        assert struct.unpack_from(">f", data, len(header) + 4 * cell)[0] == np.float32(1 + cell / 1024)
+        assert struct.unpack_from(">3f", data, v0 + 12 * cell) == (20.0, 10.0, -5.0)
+    assert len(data) == v0 + cells * 12 + 1
+    for bad in (0.0, float("nan")):
+        with pytest.raises(RangeError):
+            F.lattice_to_field(vel, bad)
+    assert F.field_file_name("Ahmed 25") == "Ahmed 25-field.vtk"
+    assert F.field_file_name("a/b:c") == "a-b-c-field.vtk"
+    assert F.field_file_name("  ") == "untitled-field.vtk"

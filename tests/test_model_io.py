@@ -267,3 +267,35 @@ def test_parse_model_sniffs_content():
     r = M.parse_model(fixture("3mf/single-object.3mf"), "x.bin")
     assert (r.format, r.unit_mm, r.item_count) == ("3mf", 1, 1)
     assert M.parse_model(b"ISO-10303-21;", "part.step").kind == "unsupported-cad"
+
+
+@pytest.mark.parametrize("path,fmt,unit", [
+    ("stl/cube-binary.stl", "stl", None), ("stl/cube-ascii-crlf.stl", "stl", None),
+    ("stl/solid-header-binary.stl", "stl", None), ("3mf/single-object.3mf", "3mf", 1),
+    ("obj/quad-cube.obj", "obj", None), ("3mf/inch.3mf", "3mf", 25.4)])
+def test_parse_model_detects_content_regardless_of_extension(path, fmt, unit):
+    """tests/unit/model/model.test.ts:6-22."""
+    r = M.parse_model(fixture(path), "misnamed.step")
+    assert (r.format, r.unit_mm, r.item_count, r.mesh.triangle_count) == (fmt, unit, 1, 12)
+
+
+@pytest.mark.parametrize("name", ["part.step", "part.STP", "part.iges", "part.IGS"])
+def test_parse_model_gives_an_export_hint_for_cad(name):
+    """model.test.ts:23-29."""
+    r = M.parse_model(b"ISO-10303-21;", name)
+    assert r.kind == "unsupported-cad" and "Export" in r.message
+
+
+def test_parse_model_keeps_errors_limits_and_dispatch():
+    """model.test.ts:30-49: STL errors survive dispatch, the triangle limit holds
+    in every format, invalid limits raise, and OBJ vertex text inside a binary
+    STL header does not change the dispatch."""
+    assert M.parse_model(fixture("stl/truncated.stl"), "bad.stl").kind == "truncated"
+    for name in ("stl/cube-binary.stl", "3mf/single-object.3mf", "obj/quad-cube.obj"):
+        assert M.parse_model(fixture(name), name, 11).kind == "too-many-triangles"
+    for limit in (-1, math.nan, 0.5):
+        with pytest.raises(RangeError):
+            M.parse_model(b"", "x", limit)
+    data = bytearray(fixture("stl/cube-binary.stl"))
+    data[:8] = b"v 0 0 0\n"
+    assert M.parse_model(bytes(data), "cube.obj").format == "stl"
