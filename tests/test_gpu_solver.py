@@ -290,7 +290,9 @@ def test_write_read_round_trip_and_totals():
 
 
 def test_ramp_matches_reference_schedule():
-    """gpu-solver.ts:119-123,401-430: start at rest, ramp u_in linearly."""
+    """gpu-solver.ts:119-123,401-430: start at rest, ramp u_in linearly by
+    rampFactor (its cases in tests/unit/stability.test.ts:155-171: 0 at step 0,
+    step / ramp on the way, 1 from the ramp's end, 1 throughout without a ramp)."""
     geometry, boundary = blob_grid("bb")
     gpu = make_solver(geometry, boundary, strict=True, ramp=20)
     ref = O.Wgsl32(32, 32, 32, 0.8, 0.06, geometry, boundary, threads=THREADS, u_in_init=0.0)
