@@ -13,6 +13,11 @@ model_fixtures.json: the reference's mesh-import fixture files
 (tests/fixtures/stl/*.stl, obj/*.obj, 3mf/*.3mf; each under 2 KB), base64, as
 inputs for the importer tests (tests/unit/stl.test.ts, obj/obj.test.ts,
 threemf/threemf.test.ts).
+
+preset_geometry.json: the SHA-256 of the reference's published preset bodies
+(public/validation/geometry/CHECKSUMS.txt: ahmed-25, cube, sphere and the
+stilts, written by its scripts/export-geometry.ts as canonical binary STL), so
+the preset generators can be checked byte for byte without the files.
 """
 import base64
 import json
@@ -48,6 +53,14 @@ def main():
     (here / "model_fixtures.json").write_text(json.dumps({"source": "tests/fixtures/{stl,obj,3mf}",
                                                           "files": files}, indent=1) + "\n")
     print("wrote model_fixtures.json with", len(files), "files")
+    sums = {}
+    for line in (ref / "public/validation/geometry/CHECKSUMS.txt").read_text().splitlines():
+        if line.strip():
+            digest, name = line.split()
+            sums[name] = digest
+    (here / "preset_geometry.json").write_text(json.dumps({"source": "public/validation/geometry/CHECKSUMS.txt",
+                                                           "sha256": sums}, indent=1) + "\n")
+    print("wrote preset_geometry.json with", len(sums), "checksums")
 
 
 if __name__ == "__main__":

@@ -62,3 +62,34 @@ def test_presets_voxelize_as_closed_surfaces():
     assert cube.watertight and cube.solid_cells == 8 * 8 * 8
     sphere = _voxelize("sphere", (32, 32, 32), 12, False)
     assert sphere.watertight and sphere.solid_cells > 0
+
+
+def _canonical_stl(mesh) -> bytes:
+    """The reference's canonical binary STL (scripts/stl-canonical.ts and
+    export-geometry.ts): an 80-byte header starting "pocketwind preset geometry",
+    the count, then per triangle a zero normal, the nine float32 coordinates
+    (negative zero written as zero) and a zero attribute."""
+    import struct
+    out = bytearray(84 + 50 * mesh.triangle_count)
+    header = b"pocketwind preset geometry"
+    out[:len(header)] = header
+    struct.pack_into("<I", out, 80, mesh.triangle_count)
+    p = mesh.positions.astype(np.float32).copy()
+    p[p == 0] = 0.0
+    for t in range(mesh.triangle_count):
+        start = 84 + 50 * t + 12
+        out[start:start + 36] = p[9 * t:9 * t + 9].astype("<f4").tobytes()
+    return bytes(out)
+
+
+def test_presets_equal_the_reference_geometry_byte_for_byte():
+    """The preset generators reproduce the reference's published bodies
+    (public/validation/geometry/*.stl, checksums in tests/golden/preset_geometry.json)."""
+    import hashlib
+    import json
+    from pathlib import Path
+    sums = json.loads((Path(__file__).parent / "golden" / "preset_geometry.json").read_text())["sha256"]
+    for name, mesh in (("ahmed-25.stl", meshes.preset_mesh("ahmed-25")), ("cube.stl", meshes.preset_mesh("cube")),
+                       ("sphere.stl", meshes.preset_mesh("sphere")),
+                       ("stilts.stl", meshes.preset_supports("ahmed-25"))):
+        assert hashlib.sha256(_canonical_stl(mesh)).hexdigest() == sums[name], name
