@@ -94,35 +94,42 @@ def test_vehicle_storage_errors_against_fp64():
         s.destroy()
 
 
-@pytest.mark.parametrize("strict", [True, False])
-def test_published_sphere_case(strict):
-    """The reference's published validation row sphere-re-100, tier S, TRT, f32
-    (docs/validation.md: Cd 1.1993, Cd voxel 1.2494; case from
-    src/validation/cases.ts:300-337 and src/app/case-run.ts) on the GPU: the
-    sphere preset at a 16-cell diameter in 128x64x64, nu = 0.008, a force
-    sample every 8 steps, 6 flow-throughs, the drag averaged over the last two.
-    The strict build equals the binary32 restatement's drag
-    (tests/golden/published_cases.json) and so the published digits; the fast
-    build stays within 5e-4 of them."""
+def _published_cases():
     import json
-    import math
     from pathlib import Path
+    return json.loads((Path(__file__).parent / "golden" / "published_cases.json").read_text())["cases"]
+
+
+@pytest.mark.parametrize("strict", [True, False])
+@pytest.mark.parametrize("key", sorted(_published_cases()))
+def test_published_sphere_case(key, strict):
+    """The reference's published validation rows sphere-re-100 with halfway walls
+    and f32 storage (docs/validation.md; case from src/validation/cases.ts:300-337
+    and src/app/case-run.ts) on the GPU: the sphere preset at a diameter of
+    nx / 8 cells, nu = 0.05 D / 100, a force sample every 8 steps, 6
+    flow-throughs, the drag averaged over the last two.  The strict TRT build
+    equals the binary32 restatement's drag (tests/golden/published_cases.json);
+    the strict builds hold the published digits within 1e-4, the fast builds
+    within 5e-4."""
+    import math
     from pocketwind_gb300 import cases, forces, meshes
     from pocketwind_gb300.geometry import voxelize
     from pocketwind_gb300.solver import GpuSolver, SolverParams
-    golden = json.loads((Path(__file__).parent / "golden" / "published_cases.json").read_text())
-    layout, diameter = (128, 64, 64), 16
+    golden = _published_cases()[key]
+    ora, pub = golden["oracle"], golden["published"]
+    layout, diameter = tuple(ora["layout"]), ora["diameter"]
+    operator = key.split(":")[1]
     body, _ = meshes.place_mesh(meshes.preset_mesh("sphere"), *layout, diameter, False)
     grid = voxelize(body, None, layout, False)
-    assert grid.frontal_cells == golden["oracle"]["frontal_cells"]
-    s = GpuSolver.create(layout, grid, SolverParams(tau0=golden["oracle"]["tau0"], u_in=0.05, strict=strict))
-    steps, window = golden["oracle"]["steps"], golden["oracle"]["average_steps"]
+    assert grid.frontal_cells == ora["frontal_cells"]
+    s = GpuSolver.create(layout, grid, SolverParams(tau0=ora["tau0"], u_in=0.05, operator=operator, strict=strict))
+    steps, window = ora["steps"], ora["average_steps"]
     fx, _, _ = forces.averaged_forces(cases.run_drag(s, steps), steps, window)
     s.destroy()
     cd = fx / (0.5 * 0.05 ** 2 * math.pi * (diameter / 2) ** 2)
     cd_voxel = fx / (0.5 * 0.05 ** 2 * grid.frontal_cells)
-    if strict:
-        assert abs(fx - golden["oracle"]["fx"]) <= 1e-9 * abs(fx)
+    if strict and operator == "trt":  # the strict TRT step equals the restatement bit for bit
+        assert abs(fx - ora["fx"]) <= 1e-9 * abs(fx)
     tol = 1e-4 if strict else 5e-4
-    assert abs(cd - golden["published"]["cd"]) <= tol
-    assert abs(cd_voxel - golden["published"]["cd_voxel"]) <= tol
+    assert abs(cd - pub["cd"]) <= tol
+    assert abs(cd_voxel - pub["cd_voxel"]) <= tol

@@ -1,23 +1,32 @@
-"""The oracle against the reference's own published run: the laminar sphere
-at tier S (docs/validation.md, sphere-re-100, 128x64x64, TRT, halfway walls,
-f32 storage: Cd 1.1993, Cd voxel 1.2494, measured by the reference on WebGPU).
-tests/golden/make_published_cases.py runs the same case on the binary32
-restatement (6 flow-throughs, about five minutes) and records both; the
-restatement matches every published digit, which pins it, and through it the
-strict GPU build that equals it bit for bit, to the reference end to end."""
+"""The oracle against the reference's own published runs: the laminar sphere at
+Re 100 (docs/validation.md, "Cases": sphere-re-100 with halfway walls and f32
+storage, measured by the reference on WebGPU).  tests/golden/make_published_cases.py
+runs the same cases on the binary32 restatement (6 flow-throughs each) and
+records both; the restatement matches every published digit, which pins it,
+and through it the strict GPU build that equals it bit for bit, to the
+reference end to end."""
 import json
 import math
 from pathlib import Path
 
-GOLDEN = json.loads((Path(__file__).parent / "golden" / "published_cases.json").read_text())
+import pytest
+
+CASES = json.loads((Path(__file__).parent / "golden" / "published_cases.json").read_text())["cases"]
+TIERS = {"S": [128, 64, 64], "M": [192, 96, 96]}
 
 
-def test_oracle_reproduces_the_published_sphere_drag():
-    pub, ora = GOLDEN["published"], GOLDEN["oracle"]
+@pytest.mark.parametrize("key", sorted(CASES))
+def test_oracle_reproduces_the_published_sphere_drag(key):
+    tier, _ = key.split(":")
+    pub, ora = CASES[key]["published"], CASES[key]["oracle"]
     # the table gives four decimals
     assert abs(ora["cd"] - pub["cd"]) <= 5e-5
     assert abs(ora["cd_voxel"] - pub["cd_voxel"]) <= 5e-5
+    # the case's set-up: diameter nx / 8, nu = 0.05 D / 100, six flow-throughs, the last two averaged
+    nx = TIERS[tier][0]
+    assert ora["layout"] == TIERS[tier] and ora["diameter"] == nx // 8
+    assert ora["tau0"] == 3 * (0.05 * (nx // 8) / 100) + 0.5
+    assert ora["steps"] == 6 * math.ceil(nx / 0.05) and ora["average_steps"] == 2 * math.ceil(nx / 0.05)
     # the two published coefficients imply the voxelized frontal area
-    area = math.pi * 8 ** 2
-    assert round(area * pub["cd"] / pub["cd_voxel"]) == ora["frontal_cells"] == 193
-    assert ora["tau0"] == 0.524 and ora["steps"] == 15360 and ora["average_steps"] == 5120
+    area = math.pi * (nx // 16) ** 2
+    assert round(area * pub["cd"] / pub["cd_voxel"]) == ora["frontal_cells"]
