@@ -14,6 +14,12 @@ model_fixtures.json: the reference's mesh-import fixture files
 inputs for the importer tests (tests/unit/stl.test.ts, obj/obj.test.ts,
 threemf/threemf.test.ts).
 
+published_results.json: from the reference's public/validation/results.json,
+the full-precision results of its laminar sphere cases (sphere-re-100: tier,
+grid, operator, walls, storage, steps, Cd, Cd voxel) and its grid-convergence
+rows (observed order, extrapolated Cd, fine-grid GCI), with the commit and date
+they were measured at.
+
 preset_geometry.json: the SHA-256 of the reference's published preset bodies
 (public/validation/geometry/CHECKSUMS.txt: ahmed-25, cube, sphere and the
 stilts, written by its scripts/export-geometry.ts as canonical binary STL), so
@@ -61,6 +67,15 @@ def main():
     (here / "preset_geometry.json").write_text(json.dumps({"source": "public/validation/geometry/CHECKSUMS.txt",
                                                            "sha256": sums}, indent=1) + "\n")
     print("wrote preset_geometry.json with", len(sums), "checksums")
+    results = json.loads((ref / "public/validation/results.json").read_text())
+    keep = ("case", "tier", "grid", "operator", "walls", "storage", "steps", "cd", "cdVoxel")
+    laminar = [{k: r[k] for k in keep} for r in results["laminar"]]
+    convergence = [{k: r[k] for k in ("case", "operator", "tiers", "kind", "order", "extrapolated", "gciFinePct")
+                    if k in r} for r in results["convergence"] if r.get("case") == "sphere-re-100"]
+    (here / "published_results.json").write_text(json.dumps({
+        "source": "public/validation/results.json", "commit": results.get("commit"), "date": results.get("date"),
+        "laminar": laminar, "convergence": convergence}, indent=1) + "\n")
+    print("wrote published_results.json with", len(laminar), "laminar rows")
 
 
 if __name__ == "__main__":
