@@ -16,9 +16,11 @@ threemf/threemf.test.ts).
 
 published_results.json: from the reference's public/validation/results.json,
 the full-precision results of its laminar sphere cases (sphere-re-100: tier,
-grid, operator, walls, storage, steps, Cd, Cd voxel) and its grid-convergence
-rows (observed order, extrapolated Cd, fine-grid GCI), with the commit and date
-they were measured at.
+grid, operator, walls, storage, steps, Cd, Cd voxel), its grid-convergence
+rows (observed order, extrapolated Cd, fine-grid GCI) and its verification
+rows (Taylor-Green errors, order and decay; Poiseuille steps to convergence,
+peak-speed and profile errors and force error), with the commit and date they
+were measured at.
 
 preset_geometry.json: the SHA-256 of the reference's published preset bodies
 (public/validation/geometry/CHECKSUMS.txt: ahmed-25, cube, sphere and the
@@ -72,9 +74,12 @@ def main():
     laminar = [{k: r[k] for k in keep} for r in results["laminar"]]
     convergence = [{k: r[k] for k in ("case", "operator", "tiers", "kind", "order", "extrapolated", "gciFinePct")
                     if k in r} for r in results["convergence"] if r.get("case") == "sphere-re-100"]
+    vkeep = ("case", "kind", "steps", "error", "observedOrder", "decayRelativeError", "errorPct", "profileErrorPct",
+             "forceError", "tau0")
+    verification = [{k: r.get(k) for k in vkeep} for r in results["verification"]]
     (here / "published_results.json").write_text(json.dumps({
         "source": "public/validation/results.json", "commit": results.get("commit"), "date": results.get("date"),
-        "laminar": laminar, "convergence": convergence}, indent=1) + "\n")
+        "laminar": laminar, "convergence": convergence, "verification": verification}, indent=1) + "\n")
     print("wrote published_results.json with", len(laminar), "laminar rows")
 
 
