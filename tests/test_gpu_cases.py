@@ -131,8 +131,9 @@ def test_published_sphere_case(key, strict):
     if strict and operator == "trt":  # the strict TRT step equals the restatement bit for bit
         assert abs(fx - ora["fx"]) <= 1e-9 * abs(fx)
     # the table's four decimals, and the reference's unrounded values
-    # (public/validation/results.json): 1e-5 relative for the strict build,
-    # as for the restatement, 5e-4 for the fast build
+    # (public/validation/results.json): for the strict build 1e-5 relative with
+    # TRT and 2e-5 with REG (the restatement: 1.4e-6 and 8e-6), 5e-4 for the
+    # fast build
     tol = 1e-4 if strict else 5e-4
     assert abs(cd - pub["cd"]) <= tol
     assert abs(cd_voxel - pub["cd_voxel"]) <= tol
@@ -141,5 +142,5 @@ def test_published_sphere_case(key, strict):
     results = json.loads((Path(__file__).parent / "golden" / "published_results.json").read_text())
     tier = key.split(":")[0]
     row = next(r for r in results["laminar"] if r["tier"] == tier and r["operator"] == operator)
-    rel = 1e-5 if strict else 5e-4
+    rel = (1e-5 if operator == "trt" else 2e-5) if strict else 5e-4
     assert abs(cd / row["cd"] - 1) < rel and abs(cd_voxel / row["cdVoxel"] - 1) < rel
