@@ -2,8 +2,9 @@
 Re 100 (docs/validation.md, "Cases": sphere-re-100 with halfway walls and f32
 storage, measured by the reference on WebGPU).  tests/golden/make_published_cases.py
 runs the same cases on the binary32 restatement (6 flow-throughs each) and
-records both; the restatement matches the published four decimals (TRT at
-tier S every digit) and the unrounded values to 1e-5, which pins it, and
+records both; the restatement matches the published values within one unit of
+their fourth decimal (TRT at tier S every digit) and the unrounded values to
+1e-5, which pins it, and
 through it the strict GPU build that equals it bit for bit, to the reference
 end to end."""
 import json
