@@ -1,11 +1,12 @@
 """Write published_cases.json: the reference's own published validation results
 for the laminar sphere (docs/validation.md, "Cases" table: sphere-re-100 with
-halfway walls and f32 storage, TRT and REG, tiers S = 128x64x64 and
-M = 192x96x96), beside the same cases run on the binary32 restatement of the
+halfway walls and f32 storage, TRT and REG, tiers S = 128x64x64,
+M = 192x96x96 and L = 256x128x128), beside the same cases run on the binary32 restatement of the
 reference's kernels in oracle/.
 
 Run from the repository root in a container that has the reference mounted
-(about five minutes per S case and twenty-five per M case on eight cores;
+(about five minutes per S case, twenty-five per M case and eighty per L case
+on eight cores;
 existing rows of the file are kept, so cases can be added one at a time):
     python tests/golden/make_published_cases.py /path/to/pocketwind [S:trt,S:reg,M:trt,M:reg]
 
@@ -32,7 +33,7 @@ import numpy as np  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 from pocketwind_gb300 import meshes  # noqa: E402
 
-TIERS = {"S": (128, 64, 64), "M": (192, 96, 96)}  # gridFor, src/validation/cases.ts:135
+TIERS = {"S": (128, 64, 64), "M": (192, 96, 96), "L": (256, 128, 128)}  # gridFor, src/validation/cases.ts:135
 U = 0.05
 
 

@@ -14,7 +14,7 @@ from pathlib import Path
 import pytest
 
 CASES = json.loads((Path(__file__).parent / "golden" / "published_cases.json").read_text())["cases"]
-TIERS = {"S": [128, 64, 64], "M": [192, 96, 96]}
+TIERS = {"S": [128, 64, 64], "M": [192, 96, 96], "L": [256, 128, 128]}
 
 
 @pytest.mark.parametrize("key", sorted(CASES))
