@@ -71,3 +71,19 @@ def test_grid_convergence_reproduces_the_published_study(operator):
     assert math.isclose(got.order, want["order"], rel_tol=1e-9)
     assert math.isclose(got.extrapolated, want["extrapolated"], rel_tol=1e-12)
     assert math.isclose(got.gci_fine_pct, want["gciFinePct"], rel_tol=1e-9)
+
+
+def test_oracle_grid_convergence_matches_the_published_study():
+    """The restatement's own drag at tiers S, M and L (TRT) gives the reference's
+    published convergence of the laminar sphere: observed order 1.3448 against
+    1.3440, extrapolated Cd 1.17626 against 1.17624, GCI 0.958% against 0.959%."""
+    from pocketwind_gb300 import reporting as R
+    keys = ("S:trt", "M:trt", "L:trt")
+    if not all(k in CASES for k in keys):
+        pytest.skip("the fixture does not hold all three TRT tiers")
+    got = R.grid_convergence([(1 / CASES[k]["oracle"]["layout"][0], CASES[k]["oracle"]["cd"]) for k in keys])
+    want = next(c for c in RESULTS["convergence"] if c["operator"] == "trt")
+    assert got.kind == "monotone"
+    assert abs(got.order - want["order"]) < 5e-3
+    assert abs(got.extrapolated - want["extrapolated"]) < 1e-4
+    assert abs(got.gci_fine_pct - want["gciFinePct"]) < 1e-2
