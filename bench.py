@@ -13,8 +13,10 @@ value   = MLUPS (million lattice-cell updates per second) of the FP16 kernel wit
           state resident in HBM, timed with CUDA events on the solver's stream.
 e2e     = the same metric through the public solver API the reference's headless
           runner uses (src/app/case-run.ts:154-169): host mesh -> GPU voxelizer ->
-          create -> {step 8, encode force, read force} loop, wall clock, with the
-          mesh upload (once) and every force readback inside the timed region.
+          create -> {step 8, encode force, read force} loop over --e2e-steps ->
+          the velocity field read to the host (read velocity, gpu-solver.ts:338),
+          wall clock, with the mesh upload, every force readback and the field
+          readback inside the timed region; setup and readback times beside it.
 roofline: the plain-cell kernels (the 32-bit cell-pair kernel, and on odd
           steps its seam-row variant), packed FP32 arithmetic, which update all
           but the wall-link and x-face cells: algorithmic bytes per cell update
@@ -213,24 +215,51 @@ def run_ours(args, rank, world):
                               "profiled_steps": min(args.steps, 200)}
         solver.destroy()
     if args.no_e2e:
-        return results, None, 0, body.positions.nbytes, cells, grid
-    # end-to-end through the public API (wall clock): mesh upload + voxelize + create + sampled stepping
+        return results, None, cells, grid
+    # end-to-end through the public API (wall clock): mesh upload + voxelize + create,
+    # then {step 8, encode force, read force} over the e2e steps, then the velocity
+    # field read back to the host (read velocity: the macro buffer, 16 bytes a cell)
     import time as _t
     barrier(world)
     t0 = _t.perf_counter()
     grid2 = voxelize(body, None, (NX, NY, NZ), True)
     solver = GpuSolver.create((NX, NY, NZ), grid2, SolverParams(tau0=TAU0, u_in=U_IN, les=True, operator="reg",
                                                                 precision="f16"))
-    samples = max(1, args.steps // 8)
-    for _ in range(samples):
-        solver.step(8)
+    t1 = _t.perf_counter()
+    samples = max(1, args.e2e_steps // 8)
+    for k in range(samples):
+        solver.step(8, k == samples - 1)
         solver.encode_force()
         f = solver.read_force()
-    e2e_s = _t.perf_counter() - t0
+    t2 = _t.perf_counter()
+    field = solver.macros()
+    t3 = _t.perf_counter()
     barrier(world)
+    finite = bool(np.isfinite(field).all())
     solver.destroy()
-    e2e_steps = samples * 8
-    return results, e2e_s, e2e_steps, body.positions.nbytes, cells, grid
+    e2e = {"total_s": t3 - t0, "setup_s": t1 - t0, "steps_s": t2 - t1, "readback_s": t3 - t2,
+           "steps": samples * 8, "samples": samples, "mesh_bytes": body.positions.nbytes,
+           "field_bytes": field.nbytes, "finite": finite}
+    return results, e2e, cells, grid
+
+
+def e2e_line(e2e, total_s, cells, world):
+    """The e2e figure: MLUPS over the whole public-API sequence (mesh upload,
+    voxelize, create, the sampled steps, the velocity field read back), with
+    the setup and readback times beside it and the same sequence's MLUPS
+    without the one-off setup."""
+    if not e2e:
+        return None
+    steps = e2e["steps"]
+    return {"value": round(job_mlups(cells, steps, world, total_s * 1e3), 2), "unit": "MLUPS",
+            "h2d_bytes_per_step": round(e2e["mesh_bytes"] / steps, 2),
+            "d2h_bytes_per_step": round((24 * e2e["samples"] + e2e["field_bytes"]) / steps, 2),
+            "steps": steps, "setup_ms": round(1e3 * e2e["setup_s"], 2),
+            "steps_ms": round(1e3 * e2e["steps_s"], 2), "read_velocity_ms": round(1e3 * e2e["readback_s"], 2),
+            "mlups_after_setup": round(job_mlups(cells, steps, world, 1e3 * (e2e["steps_s"] + e2e["readback_s"])), 2),
+            "sequence": "mesh upload + GPU voxelizer + create, then {step 8, encode force, read force} "
+                        "(macros written on the last step), then the velocity field read to the host",
+            "field_finite": e2e["finite"]}
 
 
 def accuracy_leg(steps, threads):
@@ -640,6 +669,8 @@ def main():
     ap.add_argument("--nx", type=int, default=512, help="profiling runs: the case at nx x nx/2 x nx/2")
     ap.add_argument("--only", default="f16,f32,bf16", help="profiling runs: storages to time (f16 first)")
     ap.add_argument("--no-e2e", action="store_true", help="profiling runs: skip the end-to-end leg")
+    ap.add_argument("--e2e-steps", type=int, default=2000,
+                    help="steps of the end-to-end leg (force read every 8, velocity field at the end)")
     ap.add_argument("--batch-steps", type=int, default=2000,
                     help="steps of the 64-tunnel batched leg (0 skips the leg)")
     ap.add_argument("--closure-steps", type=int, default=20480,
@@ -689,9 +720,8 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
-    results, e2e_s, e2e_steps, mesh_bytes, cells, grid = run_ours(args, rank, world)
-    ms, e2e_max = max_over_ranks([results["f16"]["ms"], e2e_s or 0.0], world)
-    e2e_s = e2e_max if e2e_s else None
+    results, e2e, cells, grid = run_ours(args, rank, world)
+    ms, e2e_max = max_over_ranks([results["f16"]["ms"], e2e["total_s"] if e2e else 0.0], world)
     if rank != 0:
         return
     peak, peak_kind = read_peaks()
@@ -740,15 +770,17 @@ def main():
                               "hbm_frac": round(cells * BYTES[p] / (r["ms"] / args.steps / 1e3) / 1e9 / peak, 4),
                               "stable": not r["unstable"]}
                           for p, r in results.items()},
-        "e2e": ({"value": round(job_mlups(cells, e2e_steps, world, e2e_s * 1e3), 2), "unit": "MLUPS",
-                 "h2d_bytes_per_step": round(mesh_bytes / e2e_steps, 2),
-                 "d2h_bytes_per_step": round(24 / 8, 2)} if e2e_s else None),
+        "e2e": e2e_line(e2e, e2e_max, cells, world),
         "gpu_launches": launches,
         "clocks": results["f16"]["clocks"],
     }
+    line["roofline"]["step_frac"] = line["step_roofline"]["frac"]
     if "f32" in line["storage_sweep"]:
         line["storage_sweep"]["f16_over_f32"] = round(line["storage_sweep"]["f16"]["mlups"] /
                                                       line["storage_sweep"]["f32"]["mlups"], 3)
+        line["roofline"]["f16_mlups"] = line["storage_sweep"]["f16"]["mlups"]
+        line["roofline"]["f32_mlups"] = line["storage_sweep"]["f32"]["mlups"]
+        line["roofline"]["f16_over_f32"] = line["storage_sweep"]["f16_over_f32"]
     if world == 1 and args.batch_steps > 0:
         line["batched_tunnels"] = batch_leg(args.batch_steps, peak=peak)
     if world == 1 and args.closure_steps > 0:

@@ -209,9 +209,13 @@ PW_API int pw_read_populations_raw(pw_domain *dom, void *out);
  * front).  pw_read_populations allocates a 19 x cells x 4-byte buffer on first
  * use; this call converts one direction and a slab of z-planes at a time through
  * a fixed 4 MiB array in the library's device image, so nx * ny must be at most
- * 1,048,576 cells (PW_ERR_INVALID otherwise).  Its first call on a device looks
- * up that array's address and should come before any stream capture; all calls
- * share the array, so calls that overlap on the GPU race. */
+ * 1,048,576 cells (PW_ERR_INVALID otherwise).  CUDA loads that code and array
+ * lazily, and loading takes device memory, so pw_domain_create loads them onto
+ * its device and looks up the array's address there: create the domain while
+ * memory is still free.  The readout's first call on a device repeats the
+ * lookup only if that failed, and should come before any stream capture.  The
+ * domain's device must be current (PW_ERR_INVALID otherwise).  All calls share
+ * the array, so calls that overlap on the GPU race. */
 PW_API int pw_read_populations_noalloc(pw_domain *dom, float *out);
 /* Replace the latest state (decoded deviations, encoded with the storage's
  * rounding, or raw codes).  Used for initial fields and checkpoint restore. */

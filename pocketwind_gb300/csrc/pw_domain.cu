@@ -157,6 +157,7 @@ struct pw_domain {
   size_t cells = 0;
   uint32_t stride = 0;
   size_t esize = 4;
+  int device = 0;                 // current device at creation: the domain's memory and streams live there
   void *f = nullptr;
   float4 *macros = nullptr;
   float4 *plane[2] = {nullptr, nullptr};
@@ -202,7 +203,8 @@ void domain_dims(const pw_domain *d, uint32_t *nx, uint32_t *ny, uint32_t *nz) {
   *nx = d->nx; *ny = d->ny; *nz = d->nz;
 }
 DomainView domain_view(const pw_domain *d) {
-  return DomainView{d->f, d->flags, d->nx, d->ny, d->nz, d->stride, d->steps, d->desc.storage, d->stream, d->slip};
+  return DomainView{d->f, d->flags, d->nx, d->ny, d->nz, d->stride, d->steps, d->desc.storage, d->stream, d->slip,
+                    d->device};
 }
 }  // namespace pwhost
 
@@ -470,6 +472,7 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
 
   pw_domain *d = new pw_domain();
   d->desc = *desc;
+  d->device = dev;
   d->nx = desc->nx; d->ny = desc->ny; d->nz = desc->nz;
   d->cells = cells;
   d->stride = (uint32_t)((cells + 63) / 64 * 64);
@@ -595,6 +598,7 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
     return rc;
   }
   a.keep = true;
+  noalloc_prepare_device();
   *out = d;
   return PW_OK;
 }

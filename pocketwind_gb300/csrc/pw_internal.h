@@ -31,8 +31,15 @@ struct DomainView {
   int storage;
   cudaStream_t stream;
   uint32_t slip;  // free-slip faces (bit 0 y, bit 1 z)
+  int device;     // the device the domain was created on
 };
 DomainView domain_view(const pw_domain *d);
+// Load the allocation-free readout's code and fixed array onto the current
+// device and look up the array's address (pw_noalloc.cu).  pw_domain_create
+// calls it, so that the readout itself never loads a module later, when the
+// device's memory may already be taken.  Failures are left for the readout
+// to report.
+void noalloc_prepare_device();
 
 // What a batch needs of a member domain (pw_batch.cu).
 struct MemberView {

@@ -16,9 +16,15 @@
 // Limits and sharing:
 //   - one x-y plane of one direction (nx * ny * 4 bytes) must fit in the 4 MiB
 //     array, i.e. nx * ny <= 1,048,576 cells; larger planes are rejected;
-//   - the first call on a device looks up the array's device address for that
-//     device (cudaGetSymbolAddress, with that device current); make that first
-//     call before any stream capture;
+//   - CUDA loads a module's code and its __device__ arrays lazily, on first
+//     use, and that load takes device memory.  So creating a domain
+//     (pw_domain_create) loads this file's readout kernels and array onto its
+//     device and looks up the array's device address for that device
+//     (cudaGetSymbolAddress, with that device current): the readout itself
+//     then loads nothing.  The readout's own first call on a device repeats
+//     the lookup only if that preparation failed; it should come before any
+//     stream capture;
+//   - the domain's device must be current when the readout is called;
 //   - every call shares the array and leaves the last call's slab in it; two
 //     calls that overlap on the GPU (from different threads or streams) race.
 #include <cuda_runtime.h>
@@ -86,7 +92,23 @@ __global__ void read_slab_kernel(pw::StepParams p, int odd_layout, int j, uint32
   slab[(size_t)blockIdx.z * p.nx * p.ny + x + (size_t)p.nx * y] = v;
 }
 
+// Force the lazy loader to bring in the three readout kernels now.
+cudaError_t load_readout_kernels() {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, read_slab_kernel<pw::STORE_F32>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, read_slab_kernel<pw::STORE_F16>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, read_slab_kernel<pw::STORE_BF16>);
+  return e;
+}
+
 }  // namespace
+
+namespace pwhost {
+void noalloc_prepare_device() {
+  void *addr = nullptr;
+  if (load_readout_kernels() != cudaSuccess || scratch_address(&addr) != PW_OK) cudaGetLastError();
+}
+}  // namespace pwhost
 
 extern "C" {
 
@@ -99,6 +121,13 @@ int pw_read_populations_noalloc(pw_domain *dom, float *out) {
     set_error("pw_read_populations_noalloc: an x-y plane of %zu cells needs %zu bytes, more than its "
               "fixed %zu-byte readout array holds (nx * ny must be at most %zu)",
               plane, plane_bytes, kScratchBytes, kScratchBytes / sizeof(float));
+    return PW_ERR_INVALID;
+  }
+  int current = -1;
+  PW_TRY(cudaGetDevice(&current));
+  if (current != v.device) {
+    set_error("pw_read_populations_noalloc: the domain lives on device %d but device %d is current; make the "
+              "domain's device current first", v.device, current);
     return PW_ERR_INVALID;
   }
   void *scratch = nullptr;

@@ -20,8 +20,10 @@ from ._lib import RangeError
 NAN_GUARD_INTERVAL = 200
 _MAX_SAFE = 2 ** 53 - 1
 
+# The instability event's text: what happened, and what a caller can change
+# (the inflow speed, or the grid resolution, which raises tau0 at a given Re).
 RUN_UNSTABLE_WHAT = "The run went unstable at step N and was reset"
-RUN_UNSTABLE_NEXT = "Lower the speed, or choose a higher tier under Advanced"
+RUN_UNSTABLE_NEXT = "Lower the inflow speed or refine the grid"
 
 
 def is_unstable_density(rho: float) -> bool:

@@ -45,7 +45,9 @@ def read_binary_stl(path: Path):
 
 
 def main():
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) < 2:
+        sys.exit(f"usage: python {Path(__file__).name} <path to the reference checkout> ...")
+    ref = Path(sys.argv[1])
     count, positions = read_binary_stl(ref / "tests/fixtures/stl/cube-binary.stl")
     here = Path(__file__).resolve().parent
     (here / "cube_binary.json").write_text(json.dumps({

@@ -70,7 +70,9 @@ def oracle_case(tier: str, operator: str):
 
 
 def main():
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) < 2:
+        sys.exit(f"usage: python {Path(__file__).name} <path to the reference checkout> ...")
+    ref = Path(sys.argv[1])
     wanted = (sys.argv[2] if len(sys.argv) > 2 else "S:trt").split(",")
     path = HERE / "published_cases.json"
     out = json.loads(path.read_text()) if path.exists() else {}

@@ -25,7 +25,7 @@ def test_reset_comes_before_the_message():
     msg = guard.reset_unstable_run(600, lambda: order.append("reset"), [lambda m: (order.append("event"), got.append(m))])
     assert order == ["reset", "event"]
     assert msg == guard.Instability(600, "The run went unstable at step 600 and was reset",
-                                    "Lower the speed, or choose a higher tier under Advanced")
+                                    "Lower the inflow speed or refine the grid")
     assert got == [msg]
 
 

@@ -8,8 +8,11 @@ through a fixed 4 MiB array in the library's device image instead of a
 it with pw_read_populations (the same decoded values, so the comparison is
 exact), on two calls in a row, on both step parities of the in-place layout,
 across several slabs per direction, and check that an oversized plane is
-rejected.  This file runs last so that a failure here leaves every other test
-already run.
+rejected.  It also reads the device's free memory before the first readout and
+after the second: creating the domain has already loaded the readout's code and
+array (CUDA loads them lazily, and loading takes memory), so the readout itself
+takes nothing.  This file runs last so that a failure here leaves every other
+test already run.
 """
 import ctypes as C
 
@@ -24,6 +27,12 @@ def _noalloc(lib):
     fn.restype = C.c_int
     fn.argtypes = [C.c_void_p, C.c_void_p]
     return fn
+
+
+def _free_device_bytes():
+    torch = pytest.importorskip("torch")
+    torch.cuda.synchronize()
+    return torch.cuda.mem_get_info()[0]
 
 
 def _solver(layout, precision):
@@ -43,12 +52,14 @@ def test_noalloc_readout_matches_allocating_readout(precision):
     # 512 x 256 planes: 512 KiB per direction plane, 8 planes per slab, 3 slabs per direction
     s = _solver((512, 256, 24), precision)
     s.step(5)  # odd layout
-    expected = s.populations()
+    expected = s.populations()  # allocates the domain's readout buffer on first use
+    free_before = _free_device_bytes()
     for _ in range(2):
         out = np.full(19 * s.cells, np.nan, np.float32)
         rc = read(s._ptr, out.ctypes.data_as(C.c_void_p))
         assert rc == _lib.PW_OK, lib.pw_last_error()
         np.testing.assert_array_equal(out, expected)
+    assert _free_device_bytes() == free_before  # nothing was allocated or loaded
     s.step(3)  # even layout
     expected = s.populations()
     out = np.full(19 * s.cells, np.nan, np.float32)
