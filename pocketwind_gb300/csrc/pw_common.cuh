@@ -183,6 +183,7 @@ struct StepParams {
   float4 *plane_out;       // this step's upstream velocity
   const uint32_t *flags;   // packed flags (kind | wall bits << 3)
   const uint32_t *special; // bit per cell: anything but plain fluid without wall links
+  const uint32_t *stored;  // bit per cell: stored by the plain kernels (plain fluid off the x faces, EQ without links)
   double *partials;        // 3 doubles per block: momentum exchange of this step's output
   uint32_t *status;        // bit 0: density guard tripped on a macro step
   uint32_t nx, ny, nz;
@@ -196,10 +197,12 @@ struct StepParams {
   // n + ld[i] and stored to element n + st[i] of f, offsets for this step's parity.
   int64_t ld[19];
   int64_t st[19];
-  // The same offsets in bytes (element offsets times the element size), added
-  // to a per-thread base pointer by the cell-pair kernel.
-  int64_t ldb[19];
-  int64_t stb[19];
+  // The cell-pair kernels' per-direction pointers: pl[i] = f + ld[i] elements,
+  // so cell n's code of direction i is at pl[i] + n elements.  The store of
+  // direction j goes where direction opp(j) was loaded (st[j] = ld[opp(j)] in
+  // both parities).
+  char *pl[19];
+  uint32_t sms;            // multiprocessors of the device (persistent grids)
   // Interpolated walls (walls.wgsl:6-21); null qoff means halfway bounce-back.
   // qoff[n]: index of cell n's first wall-link fraction (PW_NO_Q without); q: the
   // fractions in link-rank order; hist: per link, the cell's own post-collision

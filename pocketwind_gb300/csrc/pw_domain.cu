@@ -38,6 +38,19 @@ __global__ void special_kernel(const uint32_t *flags, size_t cells, uint32_t *sp
   if ((threadIdx.x & 31) == 0 && i < cells) special[i >> 5] = word;
 }
 
+// Cells the fast build's plain kernels store: plain fluid (no wall links) off
+// the x faces, and EQ cells without wall links.
+__global__ void stored_kernel(const uint32_t *flags, uint32_t nx, size_t cells, uint32_t *stored) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t bit = 0;
+  if (i < cells) {
+    uint32_t f = flags[i];
+    bit = f == pw::EQ || (f == pw::FLUID && pw::is_plain_position((uint32_t)(i % nx), nx));
+  }
+  uint32_t word = __ballot_sync(0xffffffffu, bit);
+  if ((threadIdx.x & 31) == 0 && i < cells) stored[i >> 5] = word;
+}
+
 // The fast step's edge list: non-wall cells that are special or on the x faces,
 // except EQ cells without wall links, in ascending cell order (so its force
 // partials sum in a fixed order).
@@ -161,7 +174,8 @@ struct pw_domain {
   void *f = nullptr;
   float4 *macros = nullptr;
   float4 *plane[2] = {nullptr, nullptr};
-  uint32_t *flags = nullptr, *special = nullptr;
+  uint32_t *flags = nullptr, *special = nullptr, *stored = nullptr;
+  uint32_t sms = 1;               // multiprocessors of the domain's device
   double *partials[2] = {nullptr, nullptr};
   size_t nblocks = 0;
   double *force_dev = nullptr;
@@ -219,6 +233,8 @@ pw::StepParams params_for(const pw_domain *d, uint64_t step, float u_in, int wri
   p.plane_out = d->plane[par];
   p.flags = d->flags;
   p.special = d->special;
+  p.stored = d->stored;
+  p.sms = d->sms;
   p.partials = d->partials[par];
   p.status = d->status_dev;
   p.nx = d->nx; p.ny = d->ny; p.nz = d->nz;
@@ -246,8 +262,7 @@ pw::StepParams params_for(const pw_domain *d, uint64_t step, float u_in, int wri
     const int64_t off = pw::cx_of(i) + nx * pw::cy_of(i) + nxy * pw::cz_of(i);
     p.ld[i] = par ? pw::opp_of(i) * S - off : i * S;
     p.st[i] = par ? i * S + off : pw::opp_of(i) * S;
-    p.ldb[i] = (int64_t)p.ld[i] * (int64_t)d->esize;
-    p.stb[i] = (int64_t)p.st[i] * (int64_t)d->esize;
+    p.pl[i] = static_cast<char *>(d->f) + p.ld[i] * (int64_t)d->esize;
   }
   return p;
 }
@@ -473,6 +488,11 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
   pw_domain *d = new pw_domain();
   d->desc = *desc;
   d->device = dev;
+  {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0) d->sms = (uint32_t)sms;
+    cudaGetLastError();
+  }
   d->nx = desc->nx; d->ny = desc->ny; d->nz = desc->nz;
   d->cells = cells;
   d->stride = (uint32_t)((cells + 63) / 64 * 64);
@@ -537,6 +557,7 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
   if (e == cudaSuccess) e = a.alloc((void **)&d->plane[1], plane_n * sizeof(float4));
   if (e == cudaSuccess) e = a.alloc((void **)&d->flags, cells * 4);
   if (e == cudaSuccess) e = a.alloc((void **)&d->special, ((cells + 31) / 32 + 1) * 4);
+  if (e == cudaSuccess) e = a.alloc((void **)&d->stored, ((cells + 31) / 32 + 1) * 4);
   d->interp = desc->walls == PW_WALLS_BOUZIDI;
   if (d->interp && e == cudaSuccess) e = a.alloc((void **)&d->qoff, cells * 4);
   if (d->interp && e == cudaSuccess) e = a.alloc((void **)&d->qfrac, (grid->nfrac ? grid->nfrac : 1) * 4);
@@ -575,6 +596,7 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
     clear_slip_links_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(d->flags, d->nx, d->ny, d->nz, d->slip,
                                                                            cells);
   special_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(d->flags, cells, d->special);
+  stored_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(d->flags, d->nx, cells, d->stored);
   cudaMemcpyAsync(ff, &none, 8, cudaMemcpyHostToDevice, s);
   first_fluid_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(d->flags, cells, ff);
   cudaMemcpyAsync(&d->first_fluid, ff, 8, cudaMemcpyDeviceToHost, s);
@@ -608,7 +630,7 @@ void pw_domain_destroy(pw_domain *d) {
   cudaStreamSynchronize(d->stream);
   drop_graphs(d);
   cudaFree(d->f); cudaFree(d->macros); cudaFree(d->plane[0]); cudaFree(d->plane[1]);
-  cudaFree(d->flags); cudaFree(d->special); cudaFree(d->partials[0]); cudaFree(d->partials[1]);
+  cudaFree(d->flags); cudaFree(d->special); cudaFree(d->stored); cudaFree(d->partials[0]); cudaFree(d->partials[1]);
   cudaFree(d->force_dev); cudaFree(d->status_dev); cudaFree(d->totals_dev); cudaFree(d->scratch);
   cudaFree(d->edges);
   cudaFree(d->wall_dist);

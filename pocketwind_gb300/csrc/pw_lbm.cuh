@@ -982,30 +982,31 @@ __device__ __forceinline__ float raw_of_bits(uint32_t b) {
   return __uint_as_float(b << 16);
 }
 
+// Both codes of a 32-bit word as binary32 (.x the low code).
+template <int ST>
+__device__ __forceinline__ float2 raw_of_word(uint32_t w) {
+  if constexpr (ST == STORE_F16) {
+    __half2 h;
+    memcpy(&h, &w, sizeof(h));
+    return __half22float2(h);
+  } else {
+    return make_float2(__uint_as_float(w << 16), __uint_as_float(w & 0xffff0000u));
+  }
+}
+
+// The update and stores of a cell pair whose 19 direction values (both cells,
+// stored units) are in g: collision, rounding, the stores (direction j where
+// direction opp(j) was loaded), the outlet's upstream plane and the macros.
 template <int ST, int OP, bool LES, bool ODD>
-__device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint32_t x, uint32_t y, uint32_t z,
-                                           uint32_t ok, uint32_t eq) {
+__device__ __forceinline__ void pair_finish(const StepParams &p, uint32_t n, uint32_t x, uint32_t y, uint32_t z,
+                                            uint32_t ok, uint32_t eq, float2 *g) {
   using S = Store<ST>;
-  uint16_t *f = reinterpret_cast<uint16_t *>(p.f);
   float2 eux = f2(p.u_in), euy = f2(0.f), euz = f2(0.f);
   if ((eq & 2u) && x + 2u == p.nx) {  // the outlet is the pair's second cell (x even, nx even)
     const float4 u = p.plane_in[y + p.ny * z];
     eux.y = u.x; euy.y = u.y; euz.y = u.z;
   }
-  // one 64-bit base per thread; each direction adds its byte offset from the
-  // kernel parameters
-  const char *base = reinterpret_cast<const char *>(f) + 2 * (size_t)n;
-  float2 g[19];
-#pragma unroll
-  for (int i = 0; i < 19; i++) {
-    const uint16_t *a = reinterpret_cast<const uint16_t *>(base + p.ldb[i]);
-    if (ODD && cx_of(i) != 0) {
-      g[i] = make_float2(raw_of_bits<ST>(ld_half(a)), raw_of_bits<ST>(ld_half(a + 1)));
-    } else {
-      const uint32_t w = ld_word(a);
-      g[i] = make_float2(raw_of_bits<ST>(w & 0xffffu), raw_of_bits<ST>(w >> 16));
-    }
-  }
+  const size_t o = 2 * (size_t)n;
   float2 rho, vx, vy, vz;
   const float2 om = update_fast2<OP, LES>(p, g, rho, vx, vy, vz, S::kScale, S::kInvScale, eq, eux, euy, euz);
   // a non-finite state is stored as NaN, as the reference's GPUs store it
@@ -1020,9 +1021,9 @@ __device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint
   const uint32_t nk = n * 0x9e3779b9u, nk2 = nk + 0x9e3779b9u;
   // odd steps: the EQ cell at x = 0 pushes c_x = -1 to x = nx - 1 and the one at
   // x = nx - 1 pushes c_x = +1 to x = 0 (periodic in x, as idx_wrapped)
-  // (signed element offsets: they are added to the pointer on their own)
-  const int wrap_lo = ODD && (eq & 1u) && x == 0u ? (int)p.nx : 0;
-  const int wrap_hi = ODD && (eq & 2u) && x + 2u == p.nx ? -(int)p.nx : 0;
+  // (signed byte offsets: they are added to the pointer on their own)
+  const int wrap_lo = ODD && (eq & 1u) && x == 0u ? 2 * (int)p.nx : 0;
+  const int wrap_hi = ODD && (eq & 2u) && x + 2u == p.nx ? -2 * (int)p.nx : 0;
   // the outlet's upstream cell (x = nx - 2, the first of its pair) publishes the
   // velocity of its stored codes
   const bool pub = (ok & 1u) && x + 2u == p.nx;
@@ -1039,15 +1040,14 @@ __device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint
       mz += (float)cz_of(j) * v;
     }
   }
-  char *obase = reinterpret_cast<char *>(f) + 2 * (size_t)n;
   if (ok == 3u && !wrap_lo && !wrap_hi) {
     // both cells stored here (nearly every pair): one branch for all directions
 #pragma unroll
     for (int j = 0; j < 19; j++) {
-      uint16_t *a = reinterpret_cast<uint16_t *>(obase + p.stb[j]);
+      char *a = p.pl[opp_of(j)] + o;
       if (ODD && cx_of(j) != 0) {
         st_half(a, w[j] & 0xffffu);
-        st_half(a + 1, w[j] >> 16);
+        st_half(a + 2, w[j] >> 16);
       } else {
         st_word(a, w[j]);
       }
@@ -1055,13 +1055,13 @@ __device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint
   } else {
 #pragma unroll
     for (int j = 0; j < 19; j++) {
-      uint16_t *a = reinterpret_cast<uint16_t *>(obase + p.stb[j]);
+      char *a = p.pl[opp_of(j)] + o;
       if (ODD && cx_of(j) != 0) {
         if (ok & 1u) st_half(a + (cx_of(j) < 0 ? wrap_lo : 0), w[j] & 0xffffu);
-        if (ok & 2u) st_half(a + 1 + (cx_of(j) > 0 ? wrap_hi : 0), w[j] >> 16);
+        if (ok & 2u) st_half(a + 2 + (cx_of(j) > 0 ? wrap_hi : 0), w[j] >> 16);
       } else {
         if (ok & 1u) st_half(a, w[j] & 0xffffu);
-        if (ok & 2u) st_half(a + 1, w[j] >> 16);
+        if (ok & 2u) st_half(a + 2, w[j] >> 16);
       }
     }
   }
@@ -1076,6 +1076,26 @@ __device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint
     if (ok & 1u) p.macros[n] = make_float4(rho.x, vx.x, vy.x, vz.x);
     if (ok & 2u) p.macros[n + 1] = make_float4(rho.y, vx.y, vy.y, vz.y);
   }
+}
+
+// A cell pair of the one-shot cell-pair kernel, its codes loaded straight from HBM.
+template <int ST, int OP, bool LES, bool ODD>
+__device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint32_t x, uint32_t y, uint32_t z,
+                                           uint32_t ok, uint32_t eq) {
+  // the pair's byte offset in every direction plane; each direction's plane
+  // pointer (for this step's parity) is a kernel parameter
+  const size_t o = 2 * (size_t)n;
+  float2 g[19];
+#pragma unroll
+  for (int i = 0; i < 19; i++) {
+    const char *a = p.pl[i] + o;
+    if (ODD && cx_of(i) != 0) {
+      g[i] = make_float2(raw_of_bits<ST>(ld_half(a)), raw_of_bits<ST>(ld_half(a + 2)));
+    } else {
+      g[i] = raw_of_word<ST>(ld_word(a));
+    }
+  }
+  pair_finish<ST, OP, LES, ODD>(p, n, x, y, z, ok, eq, g);
 }
 
 template <int ST, int OP, bool LES, bool ODD>
@@ -1107,6 +1127,145 @@ __global__ void __launch_bounds__(NTHREADS, 8) aa_step_pairs(StepParams p) {
   const uint32_t z = blockIdx.z + (ODD ? 1u : 0u);
   if (y + (ODD ? 1u : 0u) >= p.ny) return;
   pair_thread<ST, OP, LES, ODD>(p, x, y, z);
+}
+
+// ---------------------------------------------------------------- pipelined cell pairs
+// The cell-pair step as a persistent grid: each warp walks 64-cell runs (the
+// work of one warp of aa_step_pairs), runs W apart for W warps in the grid,
+// and stages the next run's codes in shared memory with asynchronous 4-byte
+// copies (cp.async) while it updates the current one.  A run's loads thus
+// stay in flight through the whole update of the run before it, without
+// holding registers, where the one-shot kernel has each warp load, then
+// compute with nothing in flight.  Per direction the warp copies the 32
+// aligned words of the run (and, on odd steps, one word past either end for
+// the ten directions whose pull is one element off the word grid), so every
+// global load is an aligned 128-byte line; the shifted pairs are put together
+// from two words in shared memory.  The lanes also stage their words of the
+// special and stored masks.  Stores go to HBM from registers as in
+// aa_step_pairs.
+constexpr int kRunWords = 34;                      // words -1 .. 32 of one direction of a run
+constexpr int kPipeStage = 19 * kRunWords + 64;    // + the lanes' special and stored mask words
+constexpr int kPipeWarps = NTHREADS / 32;
+
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global.L2::256B [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+__device__ __forceinline__ uint32_t shared_addr(const void *ptr) { return (uint32_t)__cvta_generic_to_shared(ptr); }
+
+// Run u: 64 cells from x0 of row (y, z); even steps every row, odd steps the
+// rows off the periodic y and z seams.
+template <bool ODD>
+__device__ __forceinline__ void run_coords(const StepParams &p, uint32_t u, uint32_t runs, uint32_t &x0, uint32_t &y,
+                                           uint32_t &z) {
+  const uint32_t row = u / runs;
+  x0 = (u - row * runs) * 64u;
+  const uint32_t rows_y = ODD ? p.ny - 2u : p.ny;
+  z = row / rows_y;
+  y = row - z * rows_y;
+  if (ODD) {
+    y += 1u;
+    z += 1u;
+  }
+}
+
+// The ten directions whose odd-step pull is one element off the word grid:
+// c_x = +1 (they need word -1 of the run) then c_x = -1 (word 32).
+__constant__ int c_halo_dir[10] = {1, 7, 9, 13, 15, 2, 8, 10, 14, 16};
+
+// Copies of run u into the stage at shared address `stage`.
+template <bool ODD>
+__device__ __forceinline__ void issue_run(const StepParams &p, char *const *pl, uint32_t u, uint32_t runs,
+                                          uint32_t stage, uint32_t lane) {
+  uint32_t x0, y, z;
+  run_coords<ODD>(p, u, runs, x0, y, z);
+  const uint32_t n0 = x0 + p.nx * (y + p.ny * z);
+  const size_t o = 2 * (size_t)n0 + 4 * lane;
+  if (x0 + 2u * lane < p.nx) {
+#pragma unroll
+    for (int i = 0; i < 19; i++)  // the aligned word of the lane's pair (odd steps: shifted back onto the grid)
+      cp_async4(stage + 4u * (i * kRunWords + lane + 1u), pl[i] + o + (ODD ? 2 * cx_of(i) : 0));
+    const uint32_t m = (n0 + 2u * lane) >> 5;
+    cp_async4(stage + 4u * (19 * kRunWords + lane), p.special + m);
+    cp_async4(stage + 4u * (19 * kRunWords + 32 + lane), p.stored + m);
+  }
+  // one word past the run for each shifted read: word -1 where the read is
+  // from x - 1 (element n0 - 2 after the shift), word 32 where from x + 1 (n0 + 64)
+  if (ODD && lane < 10u) {
+    const int dir = c_halo_dir[lane];
+    const bool front = lane < 5u;
+    cp_async4(stage + 4u * (dir * kRunWords + (front ? 0u : 33u)), pl[dir] + 2 * (size_t)n0 + (front ? -2 : 126));
+  }
+}
+
+template <int ST>
+__device__ __forceinline__ float hi_of_word(uint32_t w) {
+  if (ST == STORE_F16) return __half2float(__ushort_as_half((unsigned short)(w >> 16)));
+  return __uint_as_float(w & 0xffff0000u);
+}
+template <int ST>
+__device__ __forceinline__ float lo_of_word(uint32_t w) {
+  if (ST == STORE_F16) return __half2float(__ushort_as_half((unsigned short)(w & 0xffffu)));
+  return __uint_as_float(w << 16);
+}
+
+template <int ST, int OP, bool LES, bool ODD>
+__device__ __forceinline__ void compute_run(const StepParams &p, uint32_t x0, uint32_t y, uint32_t z,
+                                            const uint32_t *sb, uint32_t lane) {
+  const uint32_t x = x0 + 2u * lane;
+  if (x >= p.nx) return;
+  const uint32_t n = x + p.nx * (y + p.ny * z);
+  const uint32_t sh = n & 31u;  // n and n + 1 share a mask word (n even)
+  const uint32_t ok = (sb[19 * kRunWords + 32 + lane] >> sh) & 3u;
+  const uint32_t eq = ok & (sb[19 * kRunWords + lane] >> sh);
+  if (!ok) return;
+  float2 g[19];
+#pragma unroll
+  for (int i = 0; i < 19; i++) {
+    const uint32_t *r = sb + i * kRunWords + lane;
+    if (ODD && cx_of(i) > 0) {
+      g[i] = make_float2(hi_of_word<ST>(r[0]), lo_of_word<ST>(r[1]));
+    } else if (ODD && cx_of(i) < 0) {
+      g[i] = make_float2(hi_of_word<ST>(r[1]), lo_of_word<ST>(r[2]));
+    } else {
+      g[i] = raw_of_word<ST>(r[1]);
+    }
+  }
+  pair_finish<ST, OP, LES, ODD>(p, n, x, y, z, ok, eq, g);
+}
+
+// Blocks of four warps, eight to an SM, each warp walking its runs with a
+// two-stage pipeline; units = runs x rows of this step.
+template <int ST, int OP, bool LES, bool ODD>
+__global__ void __launch_bounds__(NTHREADS, 8) aa_step_pairs_pipe(StepParams p, uint32_t runs, uint32_t units) {
+  __shared__ __align__(16) uint32_t pipe[kPipeWarps][2][kPipeStage];
+  __shared__ char *s_pl[19];
+#pragma unroll
+  for (int i = 0; i < 19; i++)
+    if (threadIdx.x == (unsigned)i) s_pl[i] = p.pl[i];
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t stride = gridDim.x * kPipeWarps;
+  const uint32_t s0 = shared_addr(pipe[warp][0]), s1 = shared_addr(pipe[warp][1]);
+  uint32_t u = blockIdx.x * kPipeWarps + warp;
+  if (u < units) issue_run<ODD>(p, s_pl, u, runs, s0, lane);
+  cp_async_commit();
+  uint32_t stage = 0;
+  for (; u < units; u += stride) {
+    const uint32_t next = u + stride;
+    if (next < units) issue_run<ODD>(p, s_pl, next, runs, stage ? s0 : s1, lane);
+    cp_async_commit();
+    cp_async_wait<1>();  // this run's copies (all but the group just issued) have landed
+    __syncwarp();
+    uint32_t x0, y, z;
+    run_coords<ODD>(p, u, runs, x0, y, z);
+    compute_run<ST, OP, LES, ODD>(p, x0, y, z, pipe[warp][stage], lane);
+    __syncwarp();        // every lane is done with this stage before it is refilled
+    stage ^= 1u;
+  }
+  cp_async_wait<0>();
 }
 
 // Odd steps on the seam rows: every row of the planes z = 0 and z = nz-1, then
@@ -1541,6 +1700,16 @@ void launch_step(const StepParams &p, int storage, int op, int les, bool odd, di
 static inline void mark(const cudaEvent_t *ev, int k, cudaStream_t s) {
   if (ev) cudaEventRecord(ev[k], s);
 }
+// The persistent cell-pair kernel over runs x rows: as many blocks as fit
+// eight to an SM, at most one warp per run.
+template <int ST, int OP, bool LES, bool ODD>
+static void launch_pairs_pipe(const StepParams &p, uint32_t runs, uint32_t rows, cudaStream_t s) {
+  const uint32_t units = runs * rows;
+  if (!units) return;
+  const uint32_t blocks = min((units + kPipeWarps - 1) / kPipeWarps, 8u * max(p.sms, 1u));
+  aa_step_pairs_pipe<ST, OP, LES, ODD><<<blocks, NTHREADS, 0, s>>>(p, runs, units);
+}
+
 template <int ST, int OP, bool LES>
 static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *list, uint32_t count, cudaStream_t s,
                         const cudaEvent_t *ev, const SideStream *side) {
@@ -1569,7 +1738,7 @@ static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *l
       mark(ev, 0, s);
       if (inner.y && inner.z) {
         if constexpr (ST != STORE_F32) {
-          if (pairs) aa_step_pairs<ST, OP, LES, true><<<inner, dim3(BX, BY), 0, s>>>(p);
+          if (pairs) launch_pairs_pipe<ST, OP, LES, true>(p, runs, (p.ny - 2u) * (p.nz - 2u), s);
           else aa_step_fast<ST, OP, LES, true><<<inner, dim3(BX, BY), 0, s>>>(p);
         } else {
           aa_step_fast<ST, OP, LES, true><<<inner, dim3(BX, BY), 0, s>>>(p);
@@ -1582,7 +1751,7 @@ static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *l
     } else {
       mark(ev, 0, s);
       if constexpr (ST != STORE_F32) {
-        if (pairs) aa_step_pairs<ST, OP, LES, false><<<dim3(runs, g.y, g.z), dim3(BX, BY), 0, s>>>(p);
+        if (pairs) launch_pairs_pipe<ST, OP, LES, false>(p, runs, p.ny * p.nz, s);
         else aa_step_fast<ST, OP, LES, false><<<dim3(runs, g.y, g.z), dim3(BX, BY), 0, s>>>(p);
       } else {
         (void)pairs;

@@ -70,6 +70,47 @@ def test_batched_members_match_solo_runs(precision):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["f32", "f16"])
+def test_batched_members_match_the_reference_fp32_path(precision):
+    """Members stepped through the batch's persistent launches against the
+    oracle directly: the binary32 restatement of the reference's WGSL kernels
+    (its A/B ping-pong, src/lbm/shaders/stream_collide.wgsl) run on each
+    member's own voxel grid.  f32: populations within 1e-5 of the largest
+    (the bound of the reference's GPU-vs-CPU browser test,
+    tests/browser/gpu-vs-cpu.spec.ts) and drag within 1e-4.  f16: within
+    twice the restatement's own f16 storage (lowbias32 rounding) distance
+    from its f32 run."""
+    from oracle import oracle as O
+    from pocketwind_gb300 import geometry
+    from pocketwind_gb300.batch import Batch
+    tunnels = [t for t in cases.batch_tunnels(24, 9) if t.layout[0] <= 96][:3]
+    assert len(tunnels) == 3
+    members = [_make(t, precision) for t in tunnels]
+    batch = Batch(members)
+    steps = 57
+    batch.step(steps, True)
+    for t, m in zip(tunnels, members):
+        grid = geometry.voxelize(t.body, None, t.layout, False)
+        ref32 = O.Wgsl32(*t.layout, t.tau0, 0.05, grid.geometry, grid.boundary_cells, threads=4)
+        for k in range(steps):
+            ref32.step(0.05, k == steps - 1)
+        want = ref32.populations()
+        got = m.populations()
+        if precision == "f32":
+            assert _norm_err(got, want) < 1e-5
+            m.encode_force()
+            f = m.read_force()
+            rf = ref32.force()
+            assert abs(f.fx - rf[0]) <= 1e-4 * abs(rf[0])
+        else:
+            ref16 = O.Wgsl32(*t.layout, t.tau0, 0.05, grid.geometry, grid.boundary_cells, storage="f16", threads=4)
+            for k in range(steps):
+                ref16.step(0.05, k == steps - 1)
+            assert _norm_err(got, want) <= 2 * _norm_err(ref16.populations(), want)
+    batch.destroy()
+
+
+@pytest.mark.gpu
 def test_tuning_keeps_a_working_shape_and_reset_restarts():
     from pocketwind_gb300.batch import Batch
     tunnels = cases.batch_tunnels(4, 7)
