@@ -46,6 +46,19 @@ __host__ __device__ constexpr float w_of(int i) {
 
 __device__ __forceinline__ bool is_wall_kind(uint32_t k) { return k >= SOLID && k <= FLOOR; }
 
+// The packed flag of a fluid cell whose only wall links are the five whose
+// pull sources lie at z - 1 (c_z = +1): the first fluid layer over a flat floor.
+__host__ __device__ constexpr uint32_t floor_links(int i = 1) {
+  return i == 19 ? 0u : ((cz_of(i) == 1 ? 1u << (3 + i) : 0u) | floor_links(i + 1));
+}
+constexpr uint32_t kFloorFlag = FLUID | floor_links();
+// A floor cell of a domain with floor rows: the z = 1 layer over an all-FLOOR
+// z = 0 plane, off the periodic y seams (those rows belong to the seam kernel
+// on odd steps).
+__host__ __device__ __forceinline__ bool is_floor_cell(uint32_t flag, uint32_t y, uint32_t z, uint32_t ny) {
+  return z == 1u && y >= 1u && y + 2u <= ny && flag == kFloorFlag;
+}
+
 // Positions whose x-neighbours are reached without the periodic wrap in x; a
 // non-special cell there is a plain cell of the fast step (the y and z seams
 // are handled in the plain kernel).
@@ -183,7 +196,6 @@ struct StepParams {
   float4 *plane_out;       // this step's upstream velocity
   const uint32_t *flags;   // packed flags (kind | wall bits << 3)
   const uint32_t *special; // bit per cell: anything but plain fluid without wall links
-  const uint32_t *stored;  // bit per cell: stored by the plain kernels (plain fluid off the x faces, EQ without links)
   double *partials;        // 3 doubles per block: momentum exchange of this step's output
   uint32_t *status;        // bit 0: density guard tripped on a macro step
   uint32_t nx, ny, nz;
@@ -202,7 +214,15 @@ struct StepParams {
   // direction j goes where direction opp(j) was loaded (st[j] = ld[opp(j)] in
   // both parities).
   char *pl[19];
-  uint32_t sms;            // multiprocessors of the device (persistent grids)
+  // The other parity's pointers: a wall link i reads the slot that nobody
+  // rewrites during the step, which is where the opposite parity pulls from
+  // (odd steps: slot i of n; even steps: slot opp(i) of n - c_i).
+  char *pw[19];
+  // Floor rows: the floor kernel updates the cells of the z = 1 rows off the
+  // y seams whose only wall links are the five floor links (is_floor_cell),
+  // and the edge kernel leaves them out.
+  uint32_t floor_rows;
+  float wall_c, wall_e;    // Werner-Wengle: (nu / (1/2))^(1/7) / 8.3 and 1 / (1 + 1/7)
   // Interpolated walls (walls.wgsl:6-21); null qoff means halfway bounce-back.
   // qoff[n]: index of cell n's first wall-link fraction (PW_NO_Q without); q: the
   // fractions in link-rank order; hist: per link, the cell's own post-collision

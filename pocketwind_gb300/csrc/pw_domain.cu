@@ -38,17 +38,10 @@ __global__ void special_kernel(const uint32_t *flags, size_t cells, uint32_t *sp
   if ((threadIdx.x & 31) == 0 && i < cells) special[i >> 5] = word;
 }
 
-// Cells the fast build's plain kernels store: plain fluid (no wall links) off
-// the x faces, and EQ cells without wall links.
-__global__ void stored_kernel(const uint32_t *flags, uint32_t nx, size_t cells, uint32_t *stored) {
-  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t bit = 0;
-  if (i < cells) {
-    uint32_t f = flags[i];
-    bit = f == pw::EQ || (f == pw::FLUID && pw::is_plain_position((uint32_t)(i % nx), nx));
-  }
-  uint32_t word = __ballot_sync(0xffffffffu, bit);
-  if ((threadIdx.x & 31) == 0 && i < cells) stored[i >> 5] = word;
+// Counts the cells of the z = 0 plane that are not FLOOR.
+__global__ void floor_plane_kernel(const uint32_t *flags, uint32_t cells, uint32_t *not_floor) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < cells && (flags[i] & 7u) != pw::FLOOR) atomicAdd(not_floor, 1u);
 }
 
 // The fast step's edge list: non-wall cells that are special or on the x faces,
@@ -174,8 +167,9 @@ struct pw_domain {
   void *f = nullptr;
   float4 *macros = nullptr;
   float4 *plane[2] = {nullptr, nullptr};
-  uint32_t *flags = nullptr, *special = nullptr, *stored = nullptr;
-  uint32_t sms = 1;               // multiprocessors of the domain's device
+  uint32_t *flags = nullptr, *special = nullptr;
+  bool floor_rows = false;        // the floor kernel updates the floor layer (is_floor_cell)
+  float wall_c = 0, wall_e = 0;   // Werner-Wengle constants of the floor cells' wall model
   double *partials[2] = {nullptr, nullptr};
   size_t nblocks = 0;
   double *force_dev = nullptr;
@@ -233,8 +227,6 @@ pw::StepParams params_for(const pw_domain *d, uint64_t step, float u_in, int wri
   p.plane_out = d->plane[par];
   p.flags = d->flags;
   p.special = d->special;
-  p.stored = d->stored;
-  p.sms = d->sms;
   p.partials = d->partials[par];
   p.status = d->status_dev;
   p.nx = d->nx; p.ny = d->ny; p.nz = d->nz;
@@ -263,7 +255,12 @@ pw::StepParams params_for(const pw_domain *d, uint64_t step, float u_in, int wri
     p.ld[i] = par ? pw::opp_of(i) * S - off : i * S;
     p.st[i] = par ? i * S + off : pw::opp_of(i) * S;
     p.pl[i] = static_cast<char *>(d->f) + p.ld[i] * (int64_t)d->esize;
+    const int64_t other = par ? i * S : pw::opp_of(i) * S - off;
+    p.pw[i] = static_cast<char *>(d->f) + other * (int64_t)d->esize;
   }
+  p.floor_rows = d->floor_rows ? 1u : 0u;
+  p.wall_c = d->wall_c;
+  p.wall_e = d->wall_e;
   return p;
 }
 
@@ -488,11 +485,6 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
   pw_domain *d = new pw_domain();
   d->desc = *desc;
   d->device = dev;
-  {
-    int sms = 0;
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0) d->sms = (uint32_t)sms;
-    cudaGetLastError();
-  }
   d->nx = desc->nx; d->ny = desc->ny; d->nz = desc->nz;
   d->cells = cells;
   d->stride = (uint32_t)((cells + 63) / 64 * 64);
@@ -557,7 +549,6 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
   if (e == cudaSuccess) e = a.alloc((void **)&d->plane[1], plane_n * sizeof(float4));
   if (e == cudaSuccess) e = a.alloc((void **)&d->flags, cells * 4);
   if (e == cudaSuccess) e = a.alloc((void **)&d->special, ((cells + 31) / 32 + 1) * 4);
-  if (e == cudaSuccess) e = a.alloc((void **)&d->stored, ((cells + 31) / 32 + 1) * 4);
   d->interp = desc->walls == PW_WALLS_BOUZIDI;
   if (d->interp && e == cudaSuccess) e = a.alloc((void **)&d->qoff, cells * 4);
   if (d->interp && e == cudaSuccess) e = a.alloc((void **)&d->qfrac, (grid->nfrac ? grid->nfrac : 1) * 4);
@@ -596,7 +587,23 @@ int pw_domain_create(const pw_domain_desc *desc, const pw_grid *grid, pw_domain 
     clear_slip_links_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(d->flags, d->nx, d->ny, d->nz, d->slip,
                                                                            cells);
   special_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(d->flags, cells, d->special);
-  stored_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(d->flags, d->nx, cells, d->stored);
+  // Floor rows: in the fast build with 16-bit storage and nx even (the cell
+  // pairs) and halfway walls, the floor kernel takes the first fluid layer over
+  // a floor when the whole z = 0 plane is FLOOR (the voxelizer's floor option).
+  if (!d->tiled && !desc->strict && desc->storage != PW_STORE_F32 && (d->nx & 1u) == 0u && !d->interp &&
+      d->ny >= 3 && d->nz >= 3) {
+    uint32_t *count = reinterpret_cast<uint32_t *>(d->status_dev) + 2, not_floor = 1;
+    const uint32_t plane = d->nx * d->ny;
+    cudaMemsetAsync(count, 0, 4, s);
+    floor_plane_kernel<<<(plane + 255) / 256, 256, 0, s>>>(d->flags, plane, count);
+    if (cudaMemcpyAsync(&not_floor, count, 4, cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+        cudaStreamSynchronize(s) == cudaSuccess)
+      d->floor_rows = not_floor == 0;
+    cudaMemsetAsync(count, 0, 4, s);
+    cudaGetLastError();
+  }
+  d->wall_c = powf(d->nu / 0.5f, 0.142857149243354797f) / 8.3f;
+  d->wall_e = 1.0f / (1.0f + 0.142857149243354797f);
   cudaMemcpyAsync(ff, &none, 8, cudaMemcpyHostToDevice, s);
   first_fluid_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(d->flags, cells, ff);
   cudaMemcpyAsync(&d->first_fluid, ff, 8, cudaMemcpyDeviceToHost, s);
@@ -630,7 +637,7 @@ void pw_domain_destroy(pw_domain *d) {
   cudaStreamSynchronize(d->stream);
   drop_graphs(d);
   cudaFree(d->f); cudaFree(d->macros); cudaFree(d->plane[0]); cudaFree(d->plane[1]);
-  cudaFree(d->flags); cudaFree(d->special); cudaFree(d->stored); cudaFree(d->partials[0]); cudaFree(d->partials[1]);
+  cudaFree(d->flags); cudaFree(d->special); cudaFree(d->partials[0]); cudaFree(d->partials[1]);
   cudaFree(d->force_dev); cudaFree(d->status_dev); cudaFree(d->totals_dev); cudaFree(d->scratch);
   cudaFree(d->edges);
   cudaFree(d->wall_dist);
@@ -897,7 +904,9 @@ MemberView member_view(const pw_domain *d) {
   return v;
 }
 pw::StepParams member_params(const pw_domain *d, uint64_t step, int write_macro) {
-  return params_for(d, step, d->u_in, write_macro);
+  pw::StepParams p = params_for(d, step, d->u_in, write_macro);
+  p.floor_rows = 0;  // a batch's edge items take the floor layer through the general path
+  return p;
 }
 void member_advance(pw_domain *d, uint64_t n) { d->steps += n; }
 }  // namespace pwhost

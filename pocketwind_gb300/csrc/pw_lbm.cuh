@@ -449,6 +449,111 @@ __device__ __forceinline__ float2 update_fast2(const StepParams &p, float2 *g, f
   }
   return om_p;
 }
+
+// The LES wall cell (stream_collide.wgsl:18-80) of cells whose only wall links
+// are the five floor links (their pull sources lie at z - 1: a flat wall
+// below), two cells at once, g in stored units.  For these links the wall
+// normal is (0, 0, 1) and the exposed weight 1/9, the slip velocity is
+// (ux, uy, 0) with unit tangent t, the link stress B has only the components
+// B_xz = -tx/2 and B_yz = -ty/2 (|B|^2 = 1/2, trace 0), and the flux
+// 2 sum_j (c_j . t)(eq_j + w_j) over the opposite links reduces to
+// rho (1 - 3 uz) |u_t| / 3.  The post-collision state is then
+//   eq_i - 9 (shear - flux) w_i c_iz (c_ix tx + c_iy ty),
+// shear = 6 * (1/9) * rho * u_tau^2 (Werner-Wengle u_tau, stream_collide.wgsl:8-12).
+__device__ __forceinline__ float floor_u_tau(const StepParams &p, float speed) {
+  const float viscous = sqrtf(2.0f * p.nu * speed);  // sqrt(nu speed / y), y = 1/2
+  if (0.5f * viscous <= 11.81f * p.nu) return viscous;
+  return exp2f(p.wall_e * __log2f(speed * p.wall_c));  // (speed (nu/y)^B / A)^(1/(1+B))
+}
+
+// What a floor cell's post-collision state depends on: density, velocity,
+// K = rd - 1.5 rho u.u, and the stress term along x and y (A tx, A ty).
+struct FloorState {
+  float2 rho, vx, vy, vz, K, atx, aty;
+};
+
+// The post-collision values of floor cells for the cells in `lanes` (bits 0
+// and 1) into g, in stored units; returns the smallest f = g + w of each cell.
+__device__ __forceinline__ float2 floor_post2(float2 *g, const FloorState &w, const float scale, uint32_t lanes) {
+  const float2 r3 = mul2(f2(3.0f), w.rho), r45 = mul2(f2(4.5f), w.rho), z2 = f2(0.0f);
+  float2 lo = f2(INFINITY);
+  const auto put = [&](int i, float2 v) {
+    if (lanes & 1u) g[i].x = v.x;
+    if (lanes & 2u) g[i].y = v.y;
+    lo = make_float2(fminf(lo.x, v.x + w_of(i) * scale), fminf(lo.y, v.y + w_of(i) * scale));
+  };
+  put(0, mul2(f2(w_of(0) * scale), w.K));
+  // pair by pair: the equilibrium along cu, plus the stress term on the eight
+  // sloped links:  9 = (1,0,1), 10 = (-1,0,-1): - A tx;  15 = (1,0,-1),
+  // 16 = (-1,0,1): + A tx;  11 = (0,1,1), 12 = (0,-1,-1): - A ty;
+  // 17 = (0,1,-1), 18 = (0,-1,1): + A ty
+#define PW_FLOOR_PAIR(I, CU, EXTRA)                                         \
+  {                                                                         \
+    const float2 cu_ = (CU);                                                \
+    const float2 ev_ = fma2(mul2(r45, cu_), cu_, w.K);                      \
+    const float2 od_ = mul2(r3, cu_);                                       \
+    put(I, fma2(f2(w_of(I) * scale), add2(ev_, od_), EXTRA));               \
+    put(I + 1, fma2(f2(w_of(I) * scale), sub2(ev_, od_), EXTRA));           \
+  }
+  PW_FLOOR_PAIR(1, w.vx, z2)
+  PW_FLOOR_PAIR(3, w.vy, z2)
+  PW_FLOOR_PAIR(5, w.vz, z2)
+  PW_FLOOR_PAIR(7, add2(w.vx, w.vy), z2)
+  PW_FLOOR_PAIR(9, add2(w.vx, w.vz), neg2(w.atx))
+  PW_FLOOR_PAIR(11, add2(w.vy, w.vz), neg2(w.aty))
+  PW_FLOOR_PAIR(13, sub2(w.vx, w.vy), z2)
+  PW_FLOOR_PAIR(15, sub2(w.vx, w.vz), w.atx)
+  PW_FLOOR_PAIR(17, sub2(w.vy, w.vz), w.aty)
+#undef PW_FLOOR_PAIR
+  return lo;
+}
+
+// The wall-model post-collision state of both cells replaces g.  Returns in
+// bits 0 and 1 the cells for which the reference keeps its plain collision
+// instead (slip speed below 1e-7, or a population the stress would make
+// negative, stream_collide.wgsl:39,76-77): the caller reloads and collides them.
+__device__ __forceinline__ uint32_t floor_wall2(const StepParams &p, float2 *g, FloorState &w, const float scale,
+                                                const float inv_scale) {
+  float2 d[10], rs = g[0];
+#pragma unroll
+  for (int k = 1; k <= 9; k++) {
+    rs = add2(rs, add2(g[2 * k - 1], g[2 * k]));
+    d[k] = sub2(g[2 * k - 1], g[2 * k]);
+  }
+  const float2 is = f2(inv_scale);
+  const float2 rd = mul2(rs, is);
+  const float2 jx = add2(add2(add2(d[1], d[4]), add2(d[5], d[7])), d[8]);
+  const float2 jy = add2(add2(add2(d[2], d[4]), sub2(d[6], d[7])), d[9]);
+  const float2 jz = sub2(add2(add2(d[3], d[5]), sub2(d[6], d[8])), d[9]);
+  w.rho = add2(f2(1.0f), rd);
+  const float2 vs = mul2(rcp2(w.rho), is);
+  w.vx = mul2(jx, vs);
+  w.vy = mul2(jy, vs);
+  w.vz = mul2(jz, vs);
+  const float2 uu = fma2(w.vx, w.vx, fma2(w.vy, w.vy, mul2(w.vz, w.vz)));
+  w.K = fma2(mul2(f2(-1.5f), w.rho), uu, rd);
+  const float2 sp2 = fma2(w.vx, w.vx, mul2(w.vy, w.vy));
+  uint32_t fb = 0u;
+#pragma unroll
+  for (int l = 0; l < 2; l++) {
+    const float q = l ? sp2.y : sp2.x;
+    const float sp = q > 0.0f ? q * rsqrtf(q) : 0.0f;
+    const float r = l ? w.rho.y : w.rho.x, uz = l ? w.vz.y : w.vz.x;
+    if (!(sp >= 1e-7f)) fb |= 1u << l;  // also a NaN speed
+    const float inv = __fdividef(1.0f, sp);
+    const float ut = floor_u_tau(p, sp);
+    const float shear = (2.0f / 3.0f) * r * ut * ut;
+    const float flux = (1.0f / 3.0f) * r * (1.0f - 3.0f * uz) * sp;
+    const float a = 9.0f * (shear - flux) * (w_of(7) * scale) * inv;
+    if (l) { w.atx.y = a * w.vx.y; w.aty.y = a * w.vy.y; }
+    else { w.atx.x = a * w.vx.x; w.aty.x = a * w.vy.x; }
+  }
+  const float2 lo = floor_post2(g, w, scale, 3u);
+  if (!(lo.x >= 0.0f)) fb |= 1u;  // also a NaN state
+  if (!(lo.y >= 0.0f)) fb |= 2u;
+  return fb;
+}
+
 #endif
 
 // ---------------------------------------------------------------- cell addressing
@@ -997,9 +1102,15 @@ __device__ __forceinline__ float2 raw_of_word(uint32_t w) {
 // The update and stores of a cell pair whose 19 direction values (both cells,
 // stored units) are in g: collision, rounding, the stores (direction j where
 // direction opp(j) was loaded), the outlet's upstream plane and the macros.
-template <int ST, int OP, bool LES, bool ODD>
+// A cell pair's inputs read again (the floor cells' rare fallback); the pair's
+// slots are not written before its stores, so a second read returns them.
+struct NoReload {
+  __device__ __forceinline__ void operator()(float2 *) const {}
+};
+
+template <int ST, int OP, bool LES, bool ODD, bool FLOOR = false, class Reload = NoReload>
 __device__ __forceinline__ void pair_finish(const StepParams &p, uint32_t n, uint32_t x, uint32_t y, uint32_t z,
-                                            uint32_t ok, uint32_t eq, float2 *g) {
+                                            uint32_t ok, uint32_t eq, float2 *g, const Reload &reload = Reload()) {
   using S = Store<ST>;
   float2 eux = f2(p.u_in), euy = f2(0.f), euz = f2(0.f);
   if ((eq & 2u) && x + 2u == p.nx) {  // the outlet is the pair's second cell (x even, nx even)
@@ -1007,8 +1118,24 @@ __device__ __forceinline__ void pair_finish(const StepParams &p, uint32_t n, uin
     eux.y = u.x; euy.y = u.y; euz.y = u.z;
   }
   const size_t o = 2 * (size_t)n;
-  float2 rho, vx, vy, vz;
-  const float2 om = update_fast2<OP, LES>(p, g, rho, vx, vy, vz, S::kScale, S::kInvScale, eq, eux, euy, euz);
+  float2 rho, vx, vy, vz, om;
+  if constexpr (FLOOR && LES) {
+    // floor cells: the reference's LES wall cell; a cell for which it keeps
+    // the plain collision takes that instead (rare: no slip, or a population
+    // the wall stress would make negative)
+    FloorState w;
+    const uint32_t fb = floor_wall2(p, g, w, S::kScale, S::kInvScale);
+    rho = w.rho; vx = w.vx; vy = w.vy; vz = w.vz;
+    om = rho;  // finite exactly when the state is
+    if (fb) {
+      float2 r2, x2, y2, z2;
+      reload(g);
+      update_fast2<OP, LES>(p, g, r2, x2, y2, z2, S::kScale, S::kInvScale, 0u, eux, euy, euz);
+      floor_post2(g, w, S::kScale, ~fb & 3u);
+    }
+  } else {
+    om = update_fast2<OP, LES>(p, g, rho, vx, vy, vz, S::kScale, S::kInvScale, eq, eux, euy, euz);
+  }
   // a non-finite state is stored as NaN, as the reference's GPUs store it
   if (!(fabsf(rho.x + om.x) < INFINITY)) {
 #pragma unroll
@@ -1078,24 +1205,52 @@ __device__ __forceinline__ void pair_finish(const StepParams &p, uint32_t n, uin
   }
 }
 
-// A cell pair of the one-shot cell-pair kernel, its codes loaded straight from HBM.
-template <int ST, int OP, bool LES, bool ODD>
+// Whether direction i of a cell pair is read one element off the word grid:
+// the odd steps' pulls along c_x = +-1, and for a floor cell's links (read
+// where the opposite parity pulls from) the even steps'.
+template <bool ODD, bool LINK>
+__host__ __device__ constexpr bool shifted_read(int i) {
+  return cx_of(i) != 0 && (LINK ? !ODD : ODD);
+}
+
+// A cell pair of the one-shot cell-pair kernels, its codes loaded straight
+// from HBM.  FLOOR: both cells are floor cells, whose five floor links read
+// the slots that nobody rewrites this step (halfway bounce-back).
+template <int ST, int OP, bool LES, bool ODD, bool FLOOR = false>
 __device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint32_t x, uint32_t y, uint32_t z,
                                            uint32_t ok, uint32_t eq) {
   // the pair's byte offset in every direction plane; each direction's plane
   // pointer (for this step's parity) is a kernel parameter
   const size_t o = 2 * (size_t)n;
-  float2 g[19];
+  const auto load = [&](float2 *v) {
 #pragma unroll
-  for (int i = 0; i < 19; i++) {
-    const char *a = p.pl[i] + o;
-    if (ODD && cx_of(i) != 0) {
-      g[i] = make_float2(raw_of_bits<ST>(ld_half(a)), raw_of_bits<ST>(ld_half(a + 2)));
-    } else {
-      g[i] = raw_of_word<ST>(ld_word(a));
+    for (int i = 0; i < 19; i++) {
+      const bool link = FLOOR && cz_of(i) == 1;
+      const char *a = (link ? p.pw[i] : p.pl[i]) + o;
+      if (link ? shifted_read<ODD, true>(i) : shifted_read<ODD, false>(i)) {
+        v[i] = make_float2(raw_of_bits<ST>(ld_half(a)), raw_of_bits<ST>(ld_half(a + 2)));
+      } else {
+        v[i] = raw_of_word<ST>(ld_word(a));
+      }
     }
-  }
-  pair_finish<ST, OP, LES, ODD>(p, n, x, y, z, ok, eq, g);
+  };
+  float2 g[19];
+  load(g);
+  pair_finish<ST, OP, LES, ODD, FLOOR>(p, n, x, y, z, ok, eq, g, load);
+}
+
+// The floor layer of a domain with floor rows (is_floor_cell): the z = 1 rows
+// off the y seams, a lane per cell pair; it runs beside the cell-pair kernel
+// on the side stream.  Floor cells link only to FLOOR cells, which add
+// nothing to the drag.
+template <int ST, int OP, bool LES, bool ODD>
+__global__ void __launch_bounds__(NTHREADS) aa_step_floor(StepParams p) {
+  const uint32_t x = blockIdx.x * (2 * BX) + 2u * threadIdx.x;
+  const uint32_t y = 1u + blockIdx.y * BY + threadIdx.y;
+  if (x >= p.nx || y + 2u > p.ny) return;
+  const uint32_t n = x + p.nx * (y + p.ny);
+  const uint32_t ok = (__ldg(&p.flags[n]) == kFloorFlag ? 1u : 0u) | (__ldg(&p.flags[n + 1]) == kFloorFlag ? 2u : 0u);
+  if (ok) pair_cells<ST, OP, LES, ODD, true>(p, n, x, y, 1u, ok, 0u);
 }
 
 template <int ST, int OP, bool LES, bool ODD>
@@ -1127,145 +1282,6 @@ __global__ void __launch_bounds__(NTHREADS, 8) aa_step_pairs(StepParams p) {
   const uint32_t z = blockIdx.z + (ODD ? 1u : 0u);
   if (y + (ODD ? 1u : 0u) >= p.ny) return;
   pair_thread<ST, OP, LES, ODD>(p, x, y, z);
-}
-
-// ---------------------------------------------------------------- pipelined cell pairs
-// The cell-pair step as a persistent grid: each warp walks 64-cell runs (the
-// work of one warp of aa_step_pairs), runs W apart for W warps in the grid,
-// and stages the next run's codes in shared memory with asynchronous 4-byte
-// copies (cp.async) while it updates the current one.  A run's loads thus
-// stay in flight through the whole update of the run before it, without
-// holding registers, where the one-shot kernel has each warp load, then
-// compute with nothing in flight.  Per direction the warp copies the 32
-// aligned words of the run (and, on odd steps, one word past either end for
-// the ten directions whose pull is one element off the word grid), so every
-// global load is an aligned 128-byte line; the shifted pairs are put together
-// from two words in shared memory.  The lanes also stage their words of the
-// special and stored masks.  Stores go to HBM from registers as in
-// aa_step_pairs.
-constexpr int kRunWords = 34;                      // words -1 .. 32 of one direction of a run
-constexpr int kPipeStage = 19 * kRunWords + 64;    // + the lanes' special and stored mask words
-constexpr int kPipeWarps = NTHREADS / 32;
-
-__device__ __forceinline__ void cp_async4(uint32_t dst, const void *src) {
-  asm volatile("cp.async.ca.shared.global.L2::256B [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-__device__ __forceinline__ uint32_t shared_addr(const void *ptr) { return (uint32_t)__cvta_generic_to_shared(ptr); }
-
-// Run u: 64 cells from x0 of row (y, z); even steps every row, odd steps the
-// rows off the periodic y and z seams.
-template <bool ODD>
-__device__ __forceinline__ void run_coords(const StepParams &p, uint32_t u, uint32_t runs, uint32_t &x0, uint32_t &y,
-                                           uint32_t &z) {
-  const uint32_t row = u / runs;
-  x0 = (u - row * runs) * 64u;
-  const uint32_t rows_y = ODD ? p.ny - 2u : p.ny;
-  z = row / rows_y;
-  y = row - z * rows_y;
-  if (ODD) {
-    y += 1u;
-    z += 1u;
-  }
-}
-
-// The ten directions whose odd-step pull is one element off the word grid:
-// c_x = +1 (they need word -1 of the run) then c_x = -1 (word 32).
-__constant__ int c_halo_dir[10] = {1, 7, 9, 13, 15, 2, 8, 10, 14, 16};
-
-// Copies of run u into the stage at shared address `stage`.
-template <bool ODD>
-__device__ __forceinline__ void issue_run(const StepParams &p, char *const *pl, uint32_t u, uint32_t runs,
-                                          uint32_t stage, uint32_t lane) {
-  uint32_t x0, y, z;
-  run_coords<ODD>(p, u, runs, x0, y, z);
-  const uint32_t n0 = x0 + p.nx * (y + p.ny * z);
-  const size_t o = 2 * (size_t)n0 + 4 * lane;
-  if (x0 + 2u * lane < p.nx) {
-#pragma unroll
-    for (int i = 0; i < 19; i++)  // the aligned word of the lane's pair (odd steps: shifted back onto the grid)
-      cp_async4(stage + 4u * (i * kRunWords + lane + 1u), pl[i] + o + (ODD ? 2 * cx_of(i) : 0));
-    const uint32_t m = (n0 + 2u * lane) >> 5;
-    cp_async4(stage + 4u * (19 * kRunWords + lane), p.special + m);
-    cp_async4(stage + 4u * (19 * kRunWords + 32 + lane), p.stored + m);
-  }
-  // one word past the run for each shifted read: word -1 where the read is
-  // from x - 1 (element n0 - 2 after the shift), word 32 where from x + 1 (n0 + 64)
-  if (ODD && lane < 10u) {
-    const int dir = c_halo_dir[lane];
-    const bool front = lane < 5u;
-    cp_async4(stage + 4u * (dir * kRunWords + (front ? 0u : 33u)), pl[dir] + 2 * (size_t)n0 + (front ? -2 : 126));
-  }
-}
-
-template <int ST>
-__device__ __forceinline__ float hi_of_word(uint32_t w) {
-  if (ST == STORE_F16) return __half2float(__ushort_as_half((unsigned short)(w >> 16)));
-  return __uint_as_float(w & 0xffff0000u);
-}
-template <int ST>
-__device__ __forceinline__ float lo_of_word(uint32_t w) {
-  if (ST == STORE_F16) return __half2float(__ushort_as_half((unsigned short)(w & 0xffffu)));
-  return __uint_as_float(w << 16);
-}
-
-template <int ST, int OP, bool LES, bool ODD>
-__device__ __forceinline__ void compute_run(const StepParams &p, uint32_t x0, uint32_t y, uint32_t z,
-                                            const uint32_t *sb, uint32_t lane) {
-  const uint32_t x = x0 + 2u * lane;
-  if (x >= p.nx) return;
-  const uint32_t n = x + p.nx * (y + p.ny * z);
-  const uint32_t sh = n & 31u;  // n and n + 1 share a mask word (n even)
-  const uint32_t ok = (sb[19 * kRunWords + 32 + lane] >> sh) & 3u;
-  const uint32_t eq = ok & (sb[19 * kRunWords + lane] >> sh);
-  if (!ok) return;
-  float2 g[19];
-#pragma unroll
-  for (int i = 0; i < 19; i++) {
-    const uint32_t *r = sb + i * kRunWords + lane;
-    if (ODD && cx_of(i) > 0) {
-      g[i] = make_float2(hi_of_word<ST>(r[0]), lo_of_word<ST>(r[1]));
-    } else if (ODD && cx_of(i) < 0) {
-      g[i] = make_float2(hi_of_word<ST>(r[1]), lo_of_word<ST>(r[2]));
-    } else {
-      g[i] = raw_of_word<ST>(r[1]);
-    }
-  }
-  pair_finish<ST, OP, LES, ODD>(p, n, x, y, z, ok, eq, g);
-}
-
-// Blocks of four warps, eight to an SM, each warp walking its runs with a
-// two-stage pipeline; units = runs x rows of this step.
-template <int ST, int OP, bool LES, bool ODD>
-__global__ void __launch_bounds__(NTHREADS, 8) aa_step_pairs_pipe(StepParams p, uint32_t runs, uint32_t units) {
-  __shared__ __align__(16) uint32_t pipe[kPipeWarps][2][kPipeStage];
-  __shared__ char *s_pl[19];
-#pragma unroll
-  for (int i = 0; i < 19; i++)
-    if (threadIdx.x == (unsigned)i) s_pl[i] = p.pl[i];
-  __syncthreads();
-  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const uint32_t stride = gridDim.x * kPipeWarps;
-  const uint32_t s0 = shared_addr(pipe[warp][0]), s1 = shared_addr(pipe[warp][1]);
-  uint32_t u = blockIdx.x * kPipeWarps + warp;
-  if (u < units) issue_run<ODD>(p, s_pl, u, runs, s0, lane);
-  cp_async_commit();
-  uint32_t stage = 0;
-  for (; u < units; u += stride) {
-    const uint32_t next = u + stride;
-    if (next < units) issue_run<ODD>(p, s_pl, next, runs, stage ? s0 : s1, lane);
-    cp_async_commit();
-    cp_async_wait<1>();  // this run's copies (all but the group just issued) have landed
-    __syncwarp();
-    uint32_t x0, y, z;
-    run_coords<ODD>(p, u, runs, x0, y, z);
-    compute_run<ST, OP, LES, ODD>(p, x0, y, z, pipe[warp][stage], lane);
-    __syncwarp();        // every lane is done with this stage before it is refilled
-    stage ^= 1u;
-  }
-  cp_async_wait<0>();
 }
 
 // Odd steps on the seam rows: every row of the planes z = 0 and z = nz-1, then
@@ -1327,7 +1343,10 @@ __device__ __forceinline__ void edge_block(const StepParams &p, const uint32_t *
     const uint32_t n = __ldg(&list[t]);
     uint32_t x, y, z;
     cell_coords(p, n, x, y, z);
-    general_cell<ST, OP, LES, ODD>(p, x, y, z, n, __ldg(&p.flags[n]), fx, fy, fz, force_any);
+    const uint32_t flag = __ldg(&p.flags[n]);
+    // with floor rows on, the floor kernel updates the floor layer
+    if (!(p.floor_rows && is_floor_cell(flag, y, z, p.ny)))
+      general_cell<ST, OP, LES, ODD>(p, x, y, z, n, flag, fx, fy, fz, force_any);
   }
   reduce_force_at(force_any, fx, fy, fz, p.partials, blk, tid);
 }
@@ -1700,14 +1719,18 @@ void launch_step(const StepParams &p, int storage, int op, int les, bool odd, di
 static inline void mark(const cudaEvent_t *ev, int k, cudaStream_t s) {
   if (ev) cudaEventRecord(ev[k], s);
 }
-// The persistent cell-pair kernel over runs x rows: as many blocks as fit
-// eight to an SM, at most one warp per run.
-template <int ST, int OP, bool LES, bool ODD>
-static void launch_pairs_pipe(const StepParams &p, uint32_t runs, uint32_t rows, cudaStream_t s) {
-  const uint32_t units = runs * rows;
-  if (!units) return;
-  const uint32_t blocks = min((units + kPipeWarps - 1) / kPipeWarps, 8u * max(p.sms, 1u));
-  aa_step_pairs_pipe<ST, OP, LES, ODD><<<blocks, NTHREADS, 0, s>>>(p, runs, units);
+// The floor layer's kernel, when the domain's floor rows are on (16-bit
+// storage with nx even only: the floor rows are decided at domain creation).
+template <int ST, int OP, bool LES>
+static void launch_floor(const StepParams &p, bool odd, cudaStream_t s) {
+  if constexpr (ST != STORE_F32) {
+    if (!p.floor_rows || p.ny < 3u) return;
+    const dim3 grid((p.nx + 2 * BX - 1) / (2 * BX), (p.ny - 2u + BY - 1u) / BY);
+    if (odd) aa_step_floor<ST, OP, LES, true><<<grid, dim3(BX, BY), 0, s>>>(p);
+    else aa_step_floor<ST, OP, LES, false><<<grid, dim3(BX, BY), 0, s>>>(p);
+  } else {
+    (void)p; (void)odd; (void)s;
+  }
 }
 
 template <int ST, int OP, bool LES>
@@ -1723,6 +1746,7 @@ static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *l
   if (side) {
     // launched first so their few blocks start before the plain grid fills the GPU
     if (plain && odd) aa_step_seam<ST, OP, LES><<<dim3(g.x, seam_rows(p.ny, p.nz)), BX, 0, t>>>(p);
+    launch_floor<ST, OP, LES>(p, odd, t);
     if (count) {
       unsigned blocks = (count + NTHREADS - 1) / NTHREADS;
       if (odd) aa_step_edges<ST, OP, LES, true><<<blocks, NTHREADS, 0, t>>>(p, list, count);
@@ -1738,7 +1762,7 @@ static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *l
       mark(ev, 0, s);
       if (inner.y && inner.z) {
         if constexpr (ST != STORE_F32) {
-          if (pairs) launch_pairs_pipe<ST, OP, LES, true>(p, runs, (p.ny - 2u) * (p.nz - 2u), s);
+          if (pairs) aa_step_pairs<ST, OP, LES, true><<<inner, dim3(BX, BY), 0, s>>>(p);
           else aa_step_fast<ST, OP, LES, true><<<inner, dim3(BX, BY), 0, s>>>(p);
         } else {
           aa_step_fast<ST, OP, LES, true><<<inner, dim3(BX, BY), 0, s>>>(p);
@@ -1751,7 +1775,7 @@ static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *l
     } else {
       mark(ev, 0, s);
       if constexpr (ST != STORE_F32) {
-        if (pairs) launch_pairs_pipe<ST, OP, LES, false>(p, runs, p.ny * p.nz, s);
+        if (pairs) aa_step_pairs<ST, OP, LES, false><<<dim3(runs, g.y, g.z), dim3(BX, BY), 0, s>>>(p);
         else aa_step_fast<ST, OP, LES, false><<<dim3(runs, g.y, g.z), dim3(BX, BY), 0, s>>>(p);
       } else {
         (void)pairs;
@@ -1768,6 +1792,7 @@ static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *l
     return;
   }
   mark(ev, 4, s);
+  launch_floor<ST, OP, LES>(p, odd, s);
   if (count) {
     unsigned blocks = (count + NTHREADS - 1) / NTHREADS;
     if (odd) aa_step_edges<ST, OP, LES, true><<<blocks, NTHREADS, 0, s>>>(p, list, count);
