@@ -418,7 +418,9 @@ def closure_leg(fine_steps, train_steps, threads, snapshots=8):
     reference's validation cases average them (src/validation/cases.ts:101,240),
     and device times of the fine and coarse runs are compared.  A third coarse
     run without the plain cells' eddy viscosity gives the floor that no closure
-    of this form can go below."""
+    of this form can go below.  The three coarse runs are repeated with
+    interpolated (Bouzidi) walls on the body (walls.wgsl:6-21), the wall
+    treatment that responds to the coarse grid's resolution."""
     import numpy as np
     from pocketwind_gb300 import cases, forces, solver
     from pocketwind_gb300.closure import N_PARAMS, Closure
@@ -471,12 +473,17 @@ def closure_leg(fine_steps, train_steps, threads, snapshots=8):
     w = np.zeros(N_PARAMS, np.float32)
     w[-1] = -1.0
     floor_net.params = w
-    for label, attach in (("closure", net), ("smagorinsky", None), ("no_eddy_viscosity", floor_net)):
+    # the same three with interpolated (Bouzidi) walls on the coarse grid's body
+    runs = [(label + suffix, attach, walls)
+            for suffix, walls in (("", "bb"), ("_bouzidi", "bouzidi"))
+            for label, attach in (("closure", net), ("smagorinsky", None), ("no_eddy_viscosity", floor_net))]
+    for label, attach, walls in runs:
         c = cases.vehicle_case(128)
+        c.walls = walls
         nu_c = 0.05 * c.length_cells / 640.0
         grid = c.grid()
         s = solver.GpuSolver.create(c.layout, grid, solver.SolverParams(tau0=0.5 + 3 * nu_c, u_in=0.05, les=True,
-                                                                         operator="reg"))
+                                                                         operator="reg", walls=walls))
         if attach is not None:
             attach.attach(s)
         cases.perturbed_start(s, grid, 0.05, 0.01, seed=640)

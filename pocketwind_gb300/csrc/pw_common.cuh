@@ -209,15 +209,14 @@ struct StepParams {
   // n + ld[i] and stored to element n + st[i] of f, offsets for this step's parity.
   int64_t ld[19];
   int64_t st[19];
-  // The cell-pair kernels' per-direction pointers: pl[i] = f + ld[i] elements,
-  // so cell n's code of direction i is at pl[i] + n elements.  The store of
-  // direction j goes where direction opp(j) was loaded (st[j] = ld[opp(j)] in
-  // both parities).
-  char *pl[19];
-  // The other parity's pointers: a wall link i reads the slot that nobody
-  // rewrites during the step, which is where the opposite parity pulls from
-  // (odd steps: slot i of n; even steps: slot opp(i) of n - c_i).
-  char *pw[19];
+  // The same offsets in bytes (element offsets times the element size), added
+  // to a per-thread base pointer by the cell-pair kernels.
+  int64_t ldb[19];
+  int64_t stb[19];
+  // The other parity's load offsets in bytes: a wall link i reads the slot
+  // that nobody rewrites during the step, which is where the opposite parity
+  // pulls from (odd steps: slot i of n; even steps: slot opp(i) of n - c_i).
+  int64_t wb[19];
   // Floor rows: the floor kernel updates the cells of the z = 1 rows off the
   // y seams whose only wall links are the five floor links (is_floor_cell),
   // and the edge kernel leaves them out.

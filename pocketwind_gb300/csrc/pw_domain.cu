@@ -254,9 +254,9 @@ pw::StepParams params_for(const pw_domain *d, uint64_t step, float u_in, int wri
     const int64_t off = pw::cx_of(i) + nx * pw::cy_of(i) + nxy * pw::cz_of(i);
     p.ld[i] = par ? pw::opp_of(i) * S - off : i * S;
     p.st[i] = par ? i * S + off : pw::opp_of(i) * S;
-    p.pl[i] = static_cast<char *>(d->f) + p.ld[i] * (int64_t)d->esize;
-    const int64_t other = par ? i * S : pw::opp_of(i) * S - off;
-    p.pw[i] = static_cast<char *>(d->f) + other * (int64_t)d->esize;
+    p.ldb[i] = (int64_t)p.ld[i] * (int64_t)d->esize;
+    p.stb[i] = (int64_t)p.st[i] * (int64_t)d->esize;
+    p.wb[i] = (par ? i * S : pw::opp_of(i) * S - off) * (int64_t)d->esize;
   }
   p.floor_rows = d->floor_rows ? 1u : 0u;
   p.wall_c = d->wall_c;
@@ -303,7 +303,10 @@ void interp_state(pw_domain *d, uint64_t steps, int refresh) {
   int odd = (int)(steps & 1);
   p.partials = d->partials[odd];
   if (d->desc.strict) pwstrict::launch_interp_state(p, odd, refresh, d->desc.storage, d->grid, nullptr, 0, d->stream);
-  else pwfast::launch_interp_state(p, odd, refresh, d->desc.storage, d->grid, d->edges, d->edge_count, d->stream);
+  // the partials in the numbering of the step kernels that run: the edge
+  // list's blocks (split step) or the cell tiles (closure step)
+  else if (d->split) pwfast::launch_interp_state(p, odd, refresh, d->desc.storage, d->grid, d->edges, d->edge_count, d->stream);
+  else pwfast::launch_interp_state(p, odd, refresh, d->desc.storage, d->grid, nullptr, 0, d->stream);
 }
 
 int launch_init(pw_domain *d) {
@@ -914,8 +917,8 @@ void member_advance(pw_domain *d, uint64_t n) { d->steps += n; }
 extern "C" int pw_closure_attach(pw_domain *d, const pw_closure *c) {
   if (!alive(d)) return PW_ERR_INVALID;
   if (c) {
-    if (d->desc.strict || d->tiled || !d->desc.les || d->interp) {
-      set_error("A closure needs an LES domain with halfway walls on the fast build's one-cell-per-thread path.");
+    if (d->desc.strict || d->tiled || !d->desc.les) {
+      set_error("A closure needs an LES domain on the fast build's one-cell-per-thread path.");
       return PW_ERR_INVALID;
     }
     if (!d->wall_dist) {

@@ -453,13 +453,13 @@ __device__ __forceinline__ float2 update_fast2(const StepParams &p, float2 *g, f
 // The LES wall cell (stream_collide.wgsl:18-80) of cells whose only wall links
 // are the five floor links (their pull sources lie at z - 1: a flat wall
 // below), two cells at once, g in stored units.  For these links the wall
-// normal is (0, 0, 1) and the exposed weight 1/9, the slip velocity is
+// normal is (0, 0, 1) and the exposed weight 1/18 + 4/36 = 1/6, the slip velocity is
 // (ux, uy, 0) with unit tangent t, the link stress B has only the components
 // B_xz = -tx/2 and B_yz = -ty/2 (|B|^2 = 1/2, trace 0), and the flux
 // 2 sum_j (c_j . t)(eq_j + w_j) over the opposite links reduces to
 // rho (1 - 3 uz) |u_t| / 3.  The post-collision state is then
 //   eq_i - 9 (shear - flux) w_i c_iz (c_ix tx + c_iy ty),
-// shear = 6 * (1/9) * rho * u_tau^2 (Werner-Wengle u_tau, stream_collide.wgsl:8-12).
+// shear = 6 * (1/6) * rho * u_tau^2 (Werner-Wengle u_tau, stream_collide.wgsl:8-12).
 __device__ __forceinline__ float floor_u_tau(const StepParams &p, float speed) {
   const float viscous = sqrtf(2.0f * p.nu * speed);  // sqrt(nu speed / y), y = 1/2
   if (0.5f * viscous <= 11.81f * p.nu) return viscous;
@@ -542,7 +542,7 @@ __device__ __forceinline__ uint32_t floor_wall2(const StepParams &p, float2 *g, 
     if (!(sp >= 1e-7f)) fb |= 1u << l;  // also a NaN speed
     const float inv = __fdividef(1.0f, sp);
     const float ut = floor_u_tau(p, sp);
-    const float shear = (2.0f / 3.0f) * r * ut * ut;
+    const float shear = r * ut * ut;
     const float flux = (1.0f / 3.0f) * r * (1.0f - 3.0f * uz) * sp;
     const float a = 9.0f * (shear - flux) * (w_of(7) * scale) * inv;
     if (l) { w.atx.y = a * w.vx.y; w.aty.y = a * w.vy.y; }
@@ -1100,8 +1100,8 @@ __device__ __forceinline__ float2 raw_of_word(uint32_t w) {
 }
 
 // The update and stores of a cell pair whose 19 direction values (both cells,
-// stored units) are in g: collision, rounding, the stores (direction j where
-// direction opp(j) was loaded), the outlet's upstream plane and the macros.
+// stored units) are in g: collision, rounding, the stores, the outlet's
+// upstream plane and the macros.
 // A cell pair's inputs read again (the floor cells' rare fallback); the pair's
 // slots are not written before its stores, so a second read returns them.
 struct NoReload {
@@ -1117,7 +1117,6 @@ __device__ __forceinline__ void pair_finish(const StepParams &p, uint32_t n, uin
     const float4 u = p.plane_in[y + p.ny * z];
     eux.y = u.x; euy.y = u.y; euz.y = u.z;
   }
-  const size_t o = 2 * (size_t)n;
   float2 rho, vx, vy, vz, om;
   if constexpr (FLOOR && LES) {
     // floor cells: the reference's LES wall cell; a cell for which it keeps
@@ -1167,11 +1166,12 @@ __device__ __forceinline__ void pair_finish(const StepParams &p, uint32_t n, uin
       mz += (float)cz_of(j) * v;
     }
   }
+  char *obase = reinterpret_cast<char *>(p.f) + 2 * (size_t)n;
   if (ok == 3u && !wrap_lo && !wrap_hi) {
     // both cells stored here (nearly every pair): one branch for all directions
 #pragma unroll
     for (int j = 0; j < 19; j++) {
-      char *a = p.pl[opp_of(j)] + o;
+      char *a = obase + p.stb[j];
       if (ODD && cx_of(j) != 0) {
         st_half(a, w[j] & 0xffffu);
         st_half(a + 2, w[j] >> 16);
@@ -1182,7 +1182,7 @@ __device__ __forceinline__ void pair_finish(const StepParams &p, uint32_t n, uin
   } else {
 #pragma unroll
     for (int j = 0; j < 19; j++) {
-      char *a = p.pl[opp_of(j)] + o;
+      char *a = obase + p.stb[j];
       if (ODD && cx_of(j) != 0) {
         if (ok & 1u) st_half(a + (cx_of(j) < 0 ? wrap_lo : 0), w[j] & 0xffffu);
         if (ok & 2u) st_half(a + 2 + (cx_of(j) > 0 ? wrap_hi : 0), w[j] >> 16);
@@ -1219,14 +1219,14 @@ __host__ __device__ constexpr bool shifted_read(int i) {
 template <int ST, int OP, bool LES, bool ODD, bool FLOOR = false>
 __device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint32_t x, uint32_t y, uint32_t z,
                                            uint32_t ok, uint32_t eq) {
-  // the pair's byte offset in every direction plane; each direction's plane
-  // pointer (for this step's parity) is a kernel parameter
-  const size_t o = 2 * (size_t)n;
+  // one 64-bit base per thread; each direction adds its byte offset from the
+  // kernel parameters
+  const char *base = reinterpret_cast<const char *>(p.f) + 2 * (size_t)n;
   const auto load = [&](float2 *v) {
 #pragma unroll
     for (int i = 0; i < 19; i++) {
       const bool link = FLOOR && cz_of(i) == 1;
-      const char *a = (link ? p.pw[i] : p.pl[i]) + o;
+      const char *a = base + (link ? p.wb[i] : p.ldb[i]);
       if (link ? shifted_read<ODD, true>(i) : shifted_read<ODD, false>(i)) {
         v[i] = make_float2(raw_of_bits<ST>(ld_half(a)), raw_of_bits<ST>(ld_half(a + 2)));
       } else {
@@ -1244,7 +1244,7 @@ __device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint
 // on the side stream.  Floor cells link only to FLOOR cells, which add
 // nothing to the drag.
 template <int ST, int OP, bool LES, bool ODD>
-__global__ void __launch_bounds__(NTHREADS) aa_step_floor(StepParams p) {
+__global__ void __launch_bounds__(NTHREADS, 5) aa_step_floor(StepParams p) {
   const uint32_t x = blockIdx.x * (2 * BX) + 2u * threadIdx.x;
   const uint32_t y = 1u + blockIdx.y * BY + threadIdx.y;
   if (x >= p.nx || y + 2u > p.ny) return;

@@ -168,13 +168,19 @@ def test_training_data_match_oracle():
 
 
 @pytest_gpu
-def test_untrained_closure_is_plain_smagorinsky():
+@pytest.mark.parametrize("walls", ["bb", "bouzidi"])
+def test_untrained_closure_is_plain_smagorinsky(walls):
+    """An untrained network (c = 0) attached to a domain reproduces plain
+    Smagorinsky, with halfway walls and with interpolated (Bouzidi) walls, whose
+    wall values and force the closure kernel takes through the same one-cell
+    path (walls.wgsl:6-21)."""
     from pocketwind_gb300 import cases, solver
     from pocketwind_gb300.closure import Closure
     v = cases.vehicle_case(64)
+    v.walls = walls
     grid = v.grid()
     mk = lambda: solver.GpuSolver.create(v.layout, grid, solver.SolverParams(tau0=v.tau0, u_in=0.05, les=True,
-                                                                             operator="reg"))
+                                                                             operator="reg", walls=walls))
     plain, closed = mk(), mk()
     c = Closure(5)
     c.attach(closed)
