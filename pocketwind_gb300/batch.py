@@ -4,9 +4,12 @@ No counterpart in the reference, which runs one solver at a time
 (src/app/solver-slot.ts).  Members are ``GpuSolver`` domains of the fast build
 (``strict=False``, kernel "auto"/"cell") sharing storage, collision operator and
 LES, with equal step counts and no inlet ramp in progress.  Each batch step is
-one persistent launch over all members' work, replayed from captured CUDA
-graphs; ``tune`` times the candidate launch shapes and keeps the fastest.  The
-members keep their own force, macro and readout calls.
+two persistent launches over all members' work, side by side on two streams:
+one over every member's plain cells, one over their seam rows and edge cells
+(each kernel carries only its own code path and registers; one launch that
+carried every path's registers measured 21% slower).  Steps are replayed from
+captured CUDA graphs; ``tune`` times the candidate launch shapes and keeps the
+fastest.  The members keep their own force, macro and readout calls.
 """
 from __future__ import annotations
 

@@ -12,12 +12,15 @@
 // within two coarse cells of a wall or of the x faces are left out (the wall
 // model owns the wall cells).
 //
-// Inference (closure_step): one cell per thread; a first pass takes each plain
-// LES cell's Smagorinsky state from its populations, its strain
-// S = -3 Pi_neq / (2 rho tau_s) and the nine inputs; each warp then runs the
-// network for its 32 cells as a chain of mma.sync m16n8k16 bf16 products
-// (28 per warp, layers chained in registers); the second pass is the ordinary
-// cell update with tau = tau0 + (tau_s - tau0) max(0, 1 + c).
+// Inference (closure_step): one cell per thread, 128 cells per block; a first
+// pass takes each plain LES cell's Smagorinsky state from its populations, its
+// strain S = -3 Pi_neq / (2 rho tau_s) and the nine inputs; the block then runs
+// the network for its 128 cells on the 5th-generation tensor cores: each layer
+// is one tcgen05.mma of M = 128 cells by N = 32 outputs (K = 16 inputs, or two
+// of K = 16 hidden units), bf16 operands in shared memory, binary32
+// accumulators in tensor memory, issued by one thread and read back by every
+// thread for its own cell (tcgen05.ld); the second pass is the ordinary cell
+// update with tau = tau0 + (tau_s - tau0) max(0, 1 + c).
 #define PW_NS pwclosure
 #define PW_STRICT 0
 #include <algorithm>
@@ -35,7 +38,6 @@ using namespace pwcl;
 
 namespace {
 
-constexpr int kFragWords = 48;  // per lane: W1 8, W2 16, W3 4, b1 8, b2 8, b3 1 (+3)
 constexpr int kTrainThreads = 128;
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
@@ -43,134 +45,210 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   return *reinterpret_cast<uint32_t *>(&v);
 }
 
-__device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], const uint32_t b[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+// ---------------------------------------------------------------- tensor-core operands
+// K-major operands without swizzle: 8-row x 16-byte core matrices, element
+// (row r, k) at byte (r % 8) * 16 + (r / 8) * SBO + (k / 8) * LBO + (k % 8) * 2
+// (LBO: the next 8 elements of K; SBO: the next 8 rows).
+constexpr uint32_t kLbo = 128;
+__host__ __device__ constexpr uint32_t cm_offset(uint32_t r, uint32_t k, uint32_t sbo) {
+  return (r & 7u) * 16u + (r >> 3) * sbo + (k >> 3) * kLbo + (k & 7u) * 2u;
 }
+constexpr uint32_t kSbo1 = 2 * kLbo, kSbo2 = 4 * kLbo;  // K = 16 (layer 1), K = 32 (layer 2)
+// The network's image in global memory, copied to shared memory by each block:
+// W1 (32 x 16, inputs 9..15 zero) and W2 (32 x 32) as bf16 operands, then b1,
+// b2, W3 (bf16-rounded) and b3 as binary32.
+constexpr uint32_t kImgW1 = 0, kImgW2 = 1024, kImgB1 = 3072, kImgB2 = kImgB1 + 128, kImgW3 = kImgB2 + 128,
+                   kImgB3 = kImgW3 + 128, kImgBytes = kImgB3 + 16;
+constexpr uint32_t kFragWords = 48;  // the image's buffer: 32 x 48 words (>= kImgBytes / 4)
+static_assert(kImgBytes <= 4 * 32 * kFragWords, "network image does not fit its buffer");
 
-// Per-lane operand fragments of the three layers (B = W^T, "col" layout: lane
-// (g, t) holds B[2t, 2t+1][g] and B[2t+8, 2t+9][g] of each 16 x 8 tile) and
-// the biases in the accumulator layout (columns 2t, 2t+1 of each 8-wide tile).
 __global__ void build_fragments(const float *w, uint32_t *frag) {
-  const uint32_t lane = threadIdx.x, g = lane >> 2, t = lane & 3;
-  // word k of lane l at frag[32 k + l]: a warp loads each word as one 128-byte line
-  auto put = [&](uint32_t k, uint32_t v) { frag[32 * k + lane] = v; };
-  auto w1 = [&](uint32_t n, uint32_t k) { return k < (uint32_t)kIn ? w[kW1 + n * kIn + k] : 0.0f; };
-  auto w2 = [&](uint32_t n, uint32_t k) { return w[kW2 + n * kHidden + k]; };
-  auto w3 = [&](uint32_t k) { return g == 0 ? w[kW3 + k] : 0.0f; };
-  for (uint32_t j = 0; j < 4; j++) {
-    const uint32_t n = 8 * j + g;
-    put(2 * j, pack_bf16(w1(n, 2 * t), w1(n, 2 * t + 1)));
-    put(2 * j + 1, pack_bf16(w1(n, 2 * t + 8), w1(n, 2 * t + 9)));
-    for (uint32_t kt = 0; kt < 2; kt++) {
-      const uint32_t kb = 16 * kt;
-      put(8 + (2 * j + kt) * 2, pack_bf16(w2(n, kb + 2 * t), w2(n, kb + 2 * t + 1)));
-      put(8 + (2 * j + kt) * 2 + 1, pack_bf16(w2(n, kb + 2 * t + 8), w2(n, kb + 2 * t + 9)));
-    }
-    put(28 + 2 * j, __float_as_uint(w[kB1 + 8 * j + 2 * t]));
-    put(29 + 2 * j, __float_as_uint(w[kB1 + 8 * j + 2 * t + 1]));
-    put(36 + 2 * j, __float_as_uint(w[kB2 + 8 * j + 2 * t]));
-    put(37 + 2 * j, __float_as_uint(w[kB2 + 8 * j + 2 * t + 1]));
+  unsigned char *img = reinterpret_cast<unsigned char *>(frag);
+  for (uint32_t i = threadIdx.x; i < 32u * 16u; i += blockDim.x) {
+    const uint32_t n = i >> 4, k = i & 15u;
+    const float v = k < (uint32_t)kIn ? w[kW1 + n * kIn + k] : 0.0f;
+    *reinterpret_cast<__nv_bfloat16 *>(img + kImgW1 + cm_offset(n, k, kSbo1)) = __float2bfloat16_rn(v);
   }
-  for (uint32_t kt = 0; kt < 2; kt++) {
-    put(24 + 2 * kt, pack_bf16(w3(16 * kt + 2 * t), w3(16 * kt + 2 * t + 1)));
-    put(25 + 2 * kt, pack_bf16(w3(16 * kt + 2 * t + 8), w3(16 * kt + 2 * t + 9)));
+  for (uint32_t i = threadIdx.x; i < 32u * 32u; i += blockDim.x) {
+    const uint32_t n = i >> 5, k = i & 31u;
+    *reinterpret_cast<__nv_bfloat16 *>(img + kImgW2 + cm_offset(n, k, kSbo2)) =
+        __float2bfloat16_rn(w[kW2 + n * kHidden + k]);
   }
-  put(44, __float_as_uint(w[kB3]));
-  put(45, 0u);
-  put(46, 0u);
-  put(47, 0u);
+  for (uint32_t j = threadIdx.x; j < 32u; j += blockDim.x) {
+    reinterpret_cast<float *>(img + kImgB1)[j] = w[kB1 + j];
+    reinterpret_cast<float *>(img + kImgB2)[j] = w[kB2 + j];
+    reinterpret_cast<float *>(img + kImgW3)[j] = bf16_round(w[kW3 + j]);
+  }
+  if (threadIdx.x == 0) reinterpret_cast<float *>(img + kImgB3)[0] = w[kB3];
 }
 
-// This lane's operand fragments and biases, held in registers across cells.
-struct Frag {
-  uint32_t w1[8], w2[16], w3[4];
-  float b1[8], b2[8], b3;
+// tcgen05 instruction descriptor (kind::f16): binary32 accumulator, bf16 A and
+// B, both K-major, N = 32, M = 128.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void *ptr) { return (uint32_t)__cvta_generic_to_shared(ptr); }
+// Shared-memory matrix descriptor: start, LBO, SBO (each in 16-byte units),
+// the fixed version 1 at bit 46, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3fffu) | ((uint64_t)((kLbo >> 4) & 0x3fffu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3fffu) << 32) | ((uint64_t)1 << 46);
+}
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// 32 binary32 columns from col of this thread's TMEM lane (warp w reads lanes 32w..32w+31).
+__device__ __forceinline__ void tc_load32(uint32_t taddr, float *v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+      "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 32; j++) v[j] = __uint_as_float(r[j]);
+}
+
+// Shared state of a block's network evaluation.
+struct TcShared {
+  __align__(128) unsigned char img[kImgBytes];   // the network image
+  __align__(128) unsigned char a1[128 * 32];     // layer-1 operand: 128 cells x 16 inputs, bf16
+  __align__(128) unsigned char a2[128 * 64];     // layer-2 operand: 128 cells x 32 hidden units, bf16
+  __align__(8) uint64_t bar;                     // MMA completion
+  uint32_t tmem;                                 // base of the block's 64 TMEM columns
+  uint32_t failed;                               // a completion wait ran out
 };
 
-__device__ __forceinline__ Frag load_frag(const uint32_t *frag) {
-  const uint32_t *fr = frag + (threadIdx.x & 31u);
-  Frag f;
-#pragma unroll
-  for (int k = 0; k < 8; k++) f.w1[k] = __ldg(&fr[32 * k]);
-#pragma unroll
-  for (int k = 0; k < 16; k++) f.w2[k] = __ldg(&fr[32 * (8 + k)]);
-#pragma unroll
-  for (int k = 0; k < 4; k++) f.w3[k] = __ldg(&fr[32 * (24 + k)]);
-#pragma unroll
-  for (int k = 0; k < 8; k++) {
-    f.b1[k] = __uint_as_float(__ldg(&fr[32 * (28 + k)]));
-    f.b2[k] = __uint_as_float(__ldg(&fr[32 * (36 + k)]));
+// Bounded wait on the MMA barrier's phase `parity`; false when it ran out
+// (the caller then skips the network and keeps plain Smagorinsky, c = 0).
+__device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity) {
+  for (uint32_t it = 0; it < (1u << 22); it++) {
+    uint32_t ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    if (ok) return true;
   }
-  f.b3 = __uint_as_float(__ldg(&fr[32 * 44]));
-  return f;
+  return false;
 }
 
-// The network on the 32 cells of a warp (every lane must call; `x` is this
-// lane's input row, `stage` 256 words of shared memory owned by the warp).
-__device__ float warp_mlp(const Frag &F, const float x[kIn], uint32_t *stage) {
-  const uint32_t lane = threadIdx.x & 31u, g = lane >> 2, t = lane & 3;
-  // stage the inputs: row `lane`, word k = inputs 2k, 2k+1 (inputs 9..15 are zero)
-#pragma unroll
-  for (int k = 0; k < 8; k++) {
-    const float lo = 2 * k < kIn ? x[2 * k] : 0.0f, hi = 2 * k + 1 < kIn ? x[2 * k + 1] : 0.0f;
-    stage[lane * 8 + k] = pack_bf16(lo, hi);
+// Block start: copy the image, set up the barrier, allocate 64 TMEM columns
+// (warp 0).  All 128 threads call it.
+__device__ void tc_setup(TcShared &sh, const uint32_t *frag) {
+  const uint32_t tid = threadIdx.x + 32u * threadIdx.y;
+  const uint32_t *src = frag;
+  uint32_t *dst = reinterpret_cast<uint32_t *>(sh.img);
+  for (uint32_t i = tid; i < kImgBytes / 4u; i += 128u) dst[i] = __ldg(&src[i]);
+  if (tid == 0) {
+    sh.failed = 0u;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&sh.bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  __syncwarp();
-  float out_lo[2], out_hi[2];
-#pragma unroll
-  for (int m = 0; m < 2; m++) {
-    const uint32_t r0 = 16 * m + g, r1 = r0 + 8;
-    const uint32_t a[4] = {stage[r0 * 8 + t], stage[r1 * 8 + t], stage[r0 * 8 + 4 + t], stage[r1 * 8 + 4 + t]};
-    float h[4][4];
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      h[j][0] = F.b1[2 * j]; h[j][1] = F.b1[2 * j + 1]; h[j][2] = F.b1[2 * j]; h[j][3] = F.b1[2 * j + 1];
-      mma_bf16(h[j], a, &F.w1[2 * j]);
-    }
-    uint32_t a2[2][4];
-#pragma unroll
-    for (int kt = 0; kt < 2; kt++) {
-      a2[kt][0] = pack_bf16(tanh_fast(h[2 * kt][0]), tanh_fast(h[2 * kt][1]));
-      a2[kt][1] = pack_bf16(tanh_fast(h[2 * kt][2]), tanh_fast(h[2 * kt][3]));
-      a2[kt][2] = pack_bf16(tanh_fast(h[2 * kt + 1][0]), tanh_fast(h[2 * kt + 1][1]));
-      a2[kt][3] = pack_bf16(tanh_fast(h[2 * kt + 1][2]), tanh_fast(h[2 * kt + 1][3]));
-    }
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      h[j][0] = F.b2[2 * j]; h[j][1] = F.b2[2 * j + 1]; h[j][2] = F.b2[2 * j]; h[j][3] = F.b2[2 * j + 1];
-      mma_bf16(h[j], a2[0], &F.w2[(2 * j) * 2]);
-      mma_bf16(h[j], a2[1], &F.w2[(2 * j + 1) * 2]);
-    }
-#pragma unroll
-    for (int kt = 0; kt < 2; kt++) {
-      a2[kt][0] = pack_bf16(tanh_fast(h[2 * kt][0]), tanh_fast(h[2 * kt][1]));
-      a2[kt][1] = pack_bf16(tanh_fast(h[2 * kt][2]), tanh_fast(h[2 * kt][3]));
-      a2[kt][2] = pack_bf16(tanh_fast(h[2 * kt + 1][0]), tanh_fast(h[2 * kt + 1][1]));
-      a2[kt][3] = pack_bf16(tanh_fast(h[2 * kt + 1][2]), tanh_fast(h[2 * kt + 1][3]));
-    }
-    float o[4] = {t == 0 ? F.b3 : 0.0f, 0.0f, t == 0 ? F.b3 : 0.0f, 0.0f};
-    mma_bf16(o, a2[0], &F.w3[0]);
-    mma_bf16(o, a2[1], &F.w3[2]);
-    out_lo[m] = o[0];
-    out_hi[m] = o[2];
+  if (tid < 32u) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(smem_u32(&sh.tmem))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
-  __syncwarp();
-  float *res = reinterpret_cast<float *>(stage);
-  if (t == 0) {
-#pragma unroll
-    for (int m = 0; m < 2; m++) {
-      res[16 * m + g] = out_lo[m];
-      res[16 * m + g + 8] = out_hi[m];
-    }
+  tc_before_sync();
+  __syncthreads();
+  tc_after_sync();
+}
+
+// Block end: free the TMEM columns (warp 0), after every thread's last read.
+__device__ void tc_teardown(TcShared &sh) {
+  tc_before_sync();
+  __syncthreads();
+  tc_after_sync();
+  if (threadIdx.x + 32u * threadIdx.y < 32u)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(sh.tmem) : "memory");
+}
+
+// The network on the block's 128 cells: every thread passes its cell's inputs
+// x (zeros for cells without a closure) and gets its c.  `phase` counts the
+// barrier's completions (two per call).  Rounding as forward_scalar: inputs,
+// weights and hidden activations in bf16, binary32 accumulation.
+__device__ float block_mlp(TcShared &sh, const float x[kIn], uint32_t &phase) {
+  const uint32_t tid = threadIdx.x + 32u * threadIdx.y, warp = tid >> 5;
+  const uint32_t lane_addr = sh.tmem + ((warp * 32u) << 16);
+  // layer-1 operand row: inputs 0..7 and 8..15 (9..15 zero) as two 16-byte pieces
+  {
+    uint4 lo, hi;
+    lo.x = pack_bf16(x[0], x[1]); lo.y = pack_bf16(x[2], x[3]); lo.z = pack_bf16(x[4], x[5]);
+    lo.w = pack_bf16(x[6], x[7]);
+    hi.x = pack_bf16(x[8], 0.0f); hi.y = 0u; hi.z = 0u; hi.w = 0u;
+    *reinterpret_cast<uint4 *>(sh.a1 + cm_offset(tid, 0, kSbo1)) = lo;
+    *reinterpret_cast<uint4 *>(sh.a1 + cm_offset(tid, 8, kSbo1)) = hi;
   }
-  __syncwarp();
-  const float c = res[lane];
-  __syncwarp();
-  return c;
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  tc_before_sync();
+  __syncthreads();
+  tc_after_sync();
+  const bool live = sh.failed == 0u;
+  if (tid == 0 && live) {
+    tc_mma(sh.tmem, smem_desc(smem_u32(sh.a1), kSbo1), smem_desc(smem_u32(sh.img + kImgW1), kSbo1), 0u);
+    tc_commit(&sh.bar);
+  }
+  float h[32];
+  // each warp reads TMEM only when all its lanes saw the layer complete
+  const bool done1 = __all_sync(0xffffffffu, live && tc_wait(&sh.bar, phase & 1u));
+  phase++;
+  tc_after_sync();
+  if (done1) {
+    tc_load32(lane_addr, h);
+  } else {
+    if (live) atomicOr(&sh.failed, 1u);
+#pragma unroll
+    for (int k = 0; k < 32; k++) h[k] = 0.0f;
+  }
+  const float *b1 = reinterpret_cast<const float *>(sh.img + kImgB1);
+#pragma unroll
+  for (int k = 0; k < 32; k += 8) {
+    uint4 v;
+    v.x = pack_bf16(tanh_fast(h[k] + b1[k]), tanh_fast(h[k + 1] + b1[k + 1]));
+    v.y = pack_bf16(tanh_fast(h[k + 2] + b1[k + 2]), tanh_fast(h[k + 3] + b1[k + 3]));
+    v.z = pack_bf16(tanh_fast(h[k + 4] + b1[k + 4]), tanh_fast(h[k + 5] + b1[k + 5]));
+    v.w = pack_bf16(tanh_fast(h[k + 6] + b1[k + 6]), tanh_fast(h[k + 7] + b1[k + 7]));
+    *reinterpret_cast<uint4 *>(sh.a2 + cm_offset(tid, k, kSbo2)) = v;
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  tc_before_sync();
+  __syncthreads();
+  tc_after_sync();
+  const bool live2 = sh.failed == 0u;
+  if (tid == 0 && live2) {
+    const uint32_t a2 = smem_u32(sh.a2), w2 = smem_u32(sh.img + kImgW2);
+    tc_mma(sh.tmem + 32u, smem_desc(a2, kSbo2), smem_desc(w2, kSbo2), 0u);
+    tc_mma(sh.tmem + 32u, smem_desc(a2 + 2u * kLbo, kSbo2), smem_desc(w2 + 2u * kLbo, kSbo2), 1u);
+    tc_commit(&sh.bar);
+  }
+  const bool done2 = __all_sync(0xffffffffu, live2 && tc_wait(&sh.bar, phase & 1u));
+  phase++;
+  tc_after_sync();
+  if (!done2) {
+    if (live2) atomicOr(&sh.failed, 1u);
+    return 0.0f;
+  }
+  tc_load32(lane_addr + 32u, h);
+  const float *b2 = reinterpret_cast<const float *>(sh.img + kImgB2);
+  const float *w3 = reinterpret_cast<const float *>(sh.img + kImgW3);
+  float out = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 32; k++) out = fmaf(w3[k], bf16_round(tanh_fast(h[k] + b2[k])), out);
+  return out + reinterpret_cast<const float *>(sh.img + kImgB3)[0];
 }
 
 // Records the Smagorinsky state of a cell (first pass).
@@ -203,15 +281,17 @@ __device__ __forceinline__ void cell_inputs(const StepParams &p, const float *st
   features(s, rho, st[2], st[3], st[4], wall, p.nu, nu_s, p.u_in, x);
 }
 
-// Planes of a row of tiles each block walks (the fragments stay in registers).
+// Planes of a row of tiles each block walks (the network image and the TMEM
+// columns are set up once per block).
 constexpr uint32_t kClosurePlanes = 2;
 
 template <int ST, int OP, bool ODD>
 __global__ void __launch_bounds__(128, 4) closure_step(StepParams p, const uint32_t *frag, const uint8_t *wall_dist) {
   using S = pw::Store<ST>;
   using T = typename S::T;
-  __shared__ uint32_t stage[4][256];
-  const Frag F = load_frag(frag);
+  __shared__ TcShared sh;
+  tc_setup(sh, frag);
+  uint32_t phase = 0;
   const uint32_t x = blockIdx.x * 32 + threadIdx.x;
   const uint32_t y = blockIdx.y * 4 + threadIdx.y;
   const bool in = x < p.nx && y < p.ny;
@@ -232,7 +312,7 @@ __global__ void __launch_bounds__(128, 4) closure_step(StepParams p, const uint3
       pwclosure::update_fast<OP, true, CaptureHook>(p, g, rho, vx, vy, vz, 1.0f, 1.0f, CaptureHook{st});
       cell_inputs(p, st, (float)wall_dist[n], xin);
     }
-    const float c = warp_mlp(F, xin, stage[threadIdx.y]);
+    const float c = block_mlp(sh, xin, phase);
     bool any = false;
     double fx = 0.0, fy = 0.0, fz = 0.0;
     if (in)
@@ -241,17 +321,25 @@ __global__ void __launch_bounds__(128, 4) closure_step(StepParams p, const uint3
     const size_t slot = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * z);
     pwclosure::reduce_force_at(any, fx, fy, fz, p.partials, slot, threadIdx.x + 32 * threadIdx.y);
   }
+  if (threadIdx.x == 0 && threadIdx.y == 0 && sh.failed) atomicOr(p.status, 4u);
+  tc_teardown(sh);
 }
 
-// Network outputs for given inputs through the same warp path (tests).
-__global__ void eval_kernel(const uint32_t *frag, const float *xin, uint32_t count, float *out) {
-  __shared__ uint32_t stage[4][256];
+// Network outputs for given inputs through the same tensor-core path (tests);
+// *status gets bit 0 if a completion wait ran out.
+__global__ void __launch_bounds__(128) eval_kernel(const uint32_t *frag, const float *xin, uint32_t count, float *out,
+                                                   uint32_t *status) {
+  __shared__ TcShared sh;
+  tc_setup(sh, frag);
+  uint32_t phase = 0;
   const uint32_t i = blockIdx.x * 128 + threadIdx.x;
   float x[kIn];
 #pragma unroll
   for (int k = 0; k < kIn; k++) x[k] = i < count ? xin[(size_t)i * kIn + k] : 0.0f;
-  const float c = warp_mlp(load_frag(frag), x, stage[threadIdx.x >> 5]);
+  const float c = block_mlp(sh, x, phase);
   if (i < count) out[i] = c;
+  if (threadIdx.x == 0 && sh.failed) atomicOr(status, 1u);
+  tc_teardown(sh);
 }
 
 // ---------------------------------------------------------------- wall distance
@@ -696,18 +784,27 @@ int pw_closure_eval(pw_closure *c, const float *x, uint32_t count, float *out) {
   if (!c || (!x && count) || (!out && count)) { set_error("NULL argument"); return PW_ERR_INVALID; }
   if (!count) return PW_OK;
   float *dx = nullptr, *dy = nullptr;
+  uint32_t *dstatus = nullptr, status = 0;
   PW_TRY(cudaMalloc(&dx, (size_t)count * kIn * sizeof(float)));
   cudaError_t e = cudaMalloc(&dy, (size_t)count * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&dstatus, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemsetAsync(dstatus, 0, sizeof(uint32_t), c->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x, (size_t)count * kIn * sizeof(float), cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) {
-    eval_kernel<<<(count + 127) / 128, 128, 0, c->stream>>>(c->frag, dx, count, dy);
+    eval_kernel<<<(count + 127) / 128, 128, 0, c->stream>>>(c->frag, dx, count, dy, dstatus);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(out, dy, (size_t)count * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&status, dstatus, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   cudaFree(dx);
   cudaFree(dy);
+  cudaFree(dstatus);
   if (e != cudaSuccess) return cuda_status(e, "pw_closure_eval");
+  if (status) {
+    set_error("pw_closure_eval: a tensor-core layer did not complete in time");
+    return PW_ERR_TIMEOUT;
+  }
   return PW_OK;
 }
 
