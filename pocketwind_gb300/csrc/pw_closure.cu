@@ -20,7 +20,9 @@
 // of K = 16 hidden units), bf16 operands in shared memory, binary32
 // accumulators in tensor memory, issued by one thread and read back by every
 // thread for its own cell (tcgen05.ld); the second pass is the ordinary cell
-// update with tau = tau0 + (tau_s - tau0) max(0, 1 + c).
+// update with tau = tau0 + (tau_s - tau0) max(0, 1 + c): for the regularized
+// operator the first pass's Smagorinsky post-collision state is corrected in
+// place (finish_plain_reg), for TRT the cell goes through the one-cell path again.
 #define PW_NS pwclosure
 #define PW_STRICT 0
 #include <algorithm>
@@ -281,44 +283,101 @@ __device__ __forceinline__ void cell_inputs(const StepParams &p, const float *st
   features(s, rho, st[2], st[3], st[4], wall, p.nu, nu_s, p.u_in, x);
 }
 
-// Planes of a row of tiles each block walks (the network image and the TMEM
-// columns are set up once per block).
-constexpr uint32_t kClosurePlanes = 2;
+// REG collision of a plain cell with the closure's relaxation time, from its
+// Smagorinsky post-collision state post (first pass): in the regularized
+// operator the relaxation time enters only through (1 - omega) 4.5 w_i Q_i:Pi,
+// so the closure's state is post_i + 4.5 (omega_s - omega) w_i Q_i:Pi (Q_i:Pi
+// with the trace removed, as update_fast projects it).  Then the cell's
+// rounding, stores, macros and outlet plane, as general_cell ends.
+template <int ST, bool ODD>
+__device__ __forceinline__ void finish_plain_reg(const StepParams &p, uint32_t x, uint32_t y, uint32_t z, uint32_t n,
+                                                 const float *st, float c, float *post) {
+  using S = pw::Store<ST>;
+  using T = typename S::T;
+  const float tau_s = st[0];
+  const float tau = p.tau0 + (tau_s - p.tau0) * fmaxf(0.0f, 1.0f + c);
+  const float dc = 4.5f * (__fdividef(1.0f, tau_s) - __fdividef(1.0f, tau));
+  const float pxx = st[5], pyy = st[6], pzz = st[7], pxy = st[8], pxz = st[9], pyz = st[10];
+  const float tr3 = (pxx + pyy + pzz) * (1.0f / 3.0f);
+  const float proj[10] = {-tr3,
+                          pxx - tr3,
+                          pyy - tr3,
+                          pzz - tr3,
+                          pxx + pyy + 2.0f * pxy - tr3,
+                          pxx + pzz + 2.0f * pxz - tr3,
+                          pyy + pzz + 2.0f * pyz - tr3,
+                          pxx + pyy - 2.0f * pxy - tr3,
+                          pxx + pzz - 2.0f * pxz - tr3,
+                          pyy + pzz - 2.0f * pyz - tr3};
+  post[0] = fmaf(dc * pw::w_of(0), proj[0], post[0]);
+#pragma unroll
+  for (int i = 1; i < 19; i++) post[i] = fmaf(dc * pw::w_of(i), proj[(i + 1) / 2], post[i]);
+  const float rho = st[1];
+  if (p.write_macro && !(rho >= 0.5f && rho <= 1.5f)) atomicOr(p.status, 1u);  // also catches NaN
+  T *f = reinterpret_cast<T *>(p.f);
+  const pwclosure::Nbr b = pwclosure::make_nbr(p, x, y, z);
+  T code[19];
+#pragma unroll
+  for (int j = 0; j < 19; j++) code[j] = S::encode(post[j], (uint32_t)j, n);
+#pragma unroll
+  for (int j = 0; j < 19; j++) f[ODD ? b.push(j, p.stride) : (pw::pidx)pw::opp_of(j) * p.stride + n] = code[j];
+  if (p.write_macro) p.macros[n] = make_float4(rho, st[2], st[3], st[4]);
+  if (x + 2 == p.nx) p.plane_out[y + p.ny * z] = pwclosure::outlet_velocity_of<ST>(code);
+}
 
+// A persistent grid (four blocks per SM): each block sets up the network image
+// and its TMEM columns once, then walks tiles of 32 x 4 cells of one z-plane,
+// tiles W apart for W blocks.
 template <int ST, int OP, bool ODD>
-__global__ void __launch_bounds__(128, 4) closure_step(StepParams p, const uint32_t *frag, const uint8_t *wall_dist) {
+__global__ void __launch_bounds__(128, 4) closure_step(StepParams p, const uint32_t *frag, const uint8_t *wall_dist,
+                                                       uint32_t tiles_x, uint32_t tiles_y) {
   using S = pw::Store<ST>;
   using T = typename S::T;
   __shared__ TcShared sh;
+  __shared__ float post_s[OP == pw::OP_REG ? 19 : 1][128];  // REG: plain cells' Smagorinsky post-collision state
   tc_setup(sh, frag);
   uint32_t phase = 0;
-  const uint32_t x = blockIdx.x * 32 + threadIdx.x;
-  const uint32_t y = blockIdx.y * 4 + threadIdx.y;
-  const bool in = x < p.nx && y < p.ny;
-  const uint32_t z_end = min(p.nz, (blockIdx.z + 1) * kClosurePlanes);
-  for (uint32_t z = blockIdx.z * kClosurePlanes; z < z_end; z++) {
+  const uint32_t tid = threadIdx.x + 32u * threadIdx.y;
+  const uint32_t tiles = tiles_x * tiles_y * p.nz;
+  for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const uint32_t bx = tile % tiles_x, by = (tile / tiles_x) % tiles_y, z = tile / (tiles_x * tiles_y);
+    const uint32_t x = bx * 32 + threadIdx.x;
+    const uint32_t y = by * 4 + threadIdx.y;
+    const bool in = x < p.nx && y < p.ny;
     const uint32_t n = in ? x + p.nx * (y + p.ny * z) : 0u;
     const uint32_t flag = in ? __ldg(&p.flags[n]) : (uint32_t)pw::SOLID;
-    float xin[kIn];
+    float xin[kIn], st[11];
 #pragma unroll
     for (int k = 0; k < kIn; k++) xin[k] = 0.0f;
-    if (in && flag == pw::FLUID) {  // fluid without wall links
+    const bool plain = in && flag == pw::FLUID;  // fluid without wall links
+    if (plain) {
       const T *f = reinterpret_cast<const T *>(p.f);
       const pwclosure::Nbr b = pwclosure::make_nbr(p, x, y, z);
       float g[19];
 #pragma unroll
       for (int i = 0; i < 19; i++) g[i] = S::decode(f[ODD ? b.pull(i, p.stride) : (pw::pidx)i * p.stride + n]);
-      float st[11], rho, vx, vy, vz;
+      float rho, vx, vy, vz;
       pwclosure::update_fast<OP, true, CaptureHook>(p, g, rho, vx, vy, vz, 1.0f, 1.0f, CaptureHook{st});
       cell_inputs(p, st, (float)wall_dist[n], xin);
+      if (OP == pw::OP_REG) {
+#pragma unroll
+        for (int i = 0; i < 19; i++) post_s[i][tid] = g[i];
+      }
     }
     const float c = block_mlp(sh, xin, phase);
     bool any = false;
     double fx = 0.0, fy = 0.0, fz = 0.0;
-    if (in)
+    if (OP == pw::OP_REG && plain) {
+      // single pass: the Smagorinsky state corrected to the closure's relaxation time
+      float post[19];
+#pragma unroll
+      for (int i = 0; i < 19; i++) post[i] = post_s[OP == pw::OP_REG ? i : 0][tid];
+      finish_plain_reg<ST, ODD>(p, x, y, z, n, st, c, post);
+    } else if (in) {
       pwclosure::general_cell<ST, OP, true, ODD, ClosureHook>(p, x, y, z, n, flag, fx, fy, fz, any, ClosureHook{c});
+    }
     // the partial slot of tile (x block, y block, z), as the cell kernels number them
-    const size_t slot = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * z);
+    const size_t slot = tile;
     pwclosure::reduce_force_at(any, fx, fy, fz, p.partials, slot, threadIdx.x + 32 * threadIdx.y);
   }
   if (threadIdx.x == 0 && threadIdx.y == 0 && sh.failed) atomicOr(p.status, 4u);
@@ -667,11 +726,19 @@ namespace pwclosure_host {
 void launch_closure_step(const StepParams &p, int storage, int op, bool odd, dim3 grid, const uint32_t *frag,
                          const uint8_t *wall, cudaStream_t s) {
   const dim3 blk(32, 4);
-  const dim3 g(grid.x, grid.y, (grid.z + kClosurePlanes - 1) / kClosurePlanes);
+  static int sms[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) { cudaGetLastError(); dev = 0; }
+  if (!sms[dev] && cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    sms[dev] = 1;
+  }
+  const uint32_t tiles = grid.x * grid.y * grid.z;
+  const unsigned g = (unsigned)std::min<uint32_t>(tiles, 4u * (uint32_t)std::max(sms[dev], 1));
 #define PW_CL_LAUNCH(ST, OPV)                                                                  \
   do {                                                                                        \
-    if (odd) closure_step<ST, OPV, true><<<g, blk, 0, s>>>(p, frag, wall);                    \
-    else closure_step<ST, OPV, false><<<g, blk, 0, s>>>(p, frag, wall);                       \
+    if (odd) closure_step<ST, OPV, true><<<g, blk, 0, s>>>(p, frag, wall, grid.x, grid.y);    \
+    else closure_step<ST, OPV, false><<<g, blk, 0, s>>>(p, frag, wall, grid.x, grid.y);       \
   } while (0)
   if (op == pw::OP_REG) {
     if (storage == pw::STORE_F16) PW_CL_LAUNCH(pw::STORE_F16, pw::OP_REG);
