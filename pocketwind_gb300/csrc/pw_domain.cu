@@ -47,20 +47,27 @@ __global__ void floor_plane_kernel(const uint32_t *flags, uint32_t cells, uint32
 // The fast step's edge list: non-wall cells that are special or on the x faces,
 // except EQ cells without wall links, in ascending cell order (so its force
 // partials sum in a fixed order).
+// With floor rows the list is partitioned: part 0 the other edge cells, part 1
+// the floor cells (is_floor_cell), which the floor kernel updates in a
+// domain's own step and a batch's edge items take with the rest.
 __device__ __forceinline__ bool is_edge_cell(const uint32_t *flags, const uint32_t *special, uint32_t n, uint32_t nx,
-                                             uint32_t ny, uint32_t nz) {
+                                             uint32_t ny, uint32_t nz, int floor_rows, int part) {
   const uint32_t flag = flags[n];
   if (pw::is_wall_kind(flag & 7u) || flag == pw::EQ) return false;  // EQ without wall links: plain kernels
-  return !pw::is_plain_position(n % nx, nx) || ((special[n >> 5] >> (n & 31u)) & 1u);
+  if (!pw::is_plain_position(n % nx, nx) || ((special[n >> 5] >> (n & 31u)) & 1u)) {
+    const bool floor = floor_rows && pw::is_floor_cell(flag, (n / nx) % ny, n / nx / ny, ny);
+    return part ? floor : !floor;
+  }
+  return false;
 }
 
 constexpr int kEdgeBlock = 1024;
 
 __global__ void edge_count_kernel(const uint32_t *flags, const uint32_t *special, uint32_t nx, uint32_t ny,
-                                  uint32_t nz, uint32_t cells, uint32_t *block_counts) {
+                                  uint32_t nz, uint32_t cells, int floor_rows, int part, uint32_t *block_counts) {
   __shared__ uint32_t warp_counts[kEdgeBlock / 32];
   const uint32_t n = blockIdx.x * kEdgeBlock + threadIdx.x;
-  const bool pred = n < cells && is_edge_cell(flags, special, n, nx, ny, nz);
+  const bool pred = n < cells && is_edge_cell(flags, special, n, nx, ny, nz, floor_rows, part);
   const uint32_t ballot = __ballot_sync(0xffffffffu, pred);
   if ((threadIdx.x & 31) == 0) warp_counts[threadIdx.x >> 5] = __popc(ballot);
   __syncthreads();
@@ -94,10 +101,11 @@ __global__ void edge_scan_kernel(uint32_t *counts, uint32_t nblk, uint32_t *tota
 }
 
 __global__ void edge_write_kernel(const uint32_t *flags, const uint32_t *special, uint32_t nx, uint32_t ny,
-                                  uint32_t nz, uint32_t cells, const uint32_t *offsets, uint32_t *list) {
+                                  uint32_t nz, uint32_t cells, int floor_rows, int part, const uint32_t *offsets,
+                                  uint32_t *list) {
   __shared__ uint32_t warp_base[kEdgeBlock / 32];
   const uint32_t n = blockIdx.x * kEdgeBlock + threadIdx.x;
-  const bool pred = n < cells && is_edge_cell(flags, special, n, nx, ny, nz);
+  const bool pred = n < cells && is_edge_cell(flags, special, n, nx, ny, nz, floor_rows, part);
   const uint32_t ballot = __ballot_sync(0xffffffffu, pred);
   const uint32_t lane = threadIdx.x & 31;
   if (lane == 0) warp_base[threadIdx.x >> 5] = __popc(ballot);
@@ -191,6 +199,7 @@ struct pw_domain {
   bool split = false;             // fast build, one cell per thread: plain kernel + edge list
   uint32_t *edges = nullptr;      // edge cells in ascending order
   uint32_t edge_count = 0;
+  uint32_t edge_own = 0;          // the list's head that a domain's own step runs (all but its floor cells)
   dim3 plain_grid;                // the cell grid, or empty when no plain position exists
   const uint32_t *closure_frag = nullptr;  // attached learned closure (its weight fragments)
   uint8_t *wall_dist = nullptr;   // cells to the nearest wall, for the closure's inputs
@@ -282,7 +291,7 @@ void enqueue_step(pw_domain *d, uint64_t step, float u_in, int write_macro) {
                                         d->stream);
   else if (d->split)
     pwfast::launch_step_split(p, d->desc.storage, d->desc.op, d->desc.les, odd, d->plain_grid, d->edges,
-                              d->edge_count, d->stream, nullptr, &d->side);
+                              d->edge_own, d->stream, nullptr, &d->side);
   else
     pwfast::launch_step(p, d->desc.storage, d->desc.op, d->desc.les, odd, d->grid, d->stream);
 }
@@ -398,23 +407,29 @@ cudaGraphExec_t graph_for(pw_domain *d, int start_parity, int macro_last) {
 int build_edge_list(pw_domain *d, Allocs &a) {
   const uint32_t cells = (uint32_t)d->cells;
   const uint32_t nblk = (cells + kEdgeBlock - 1) / kEdgeBlock;
-  uint32_t *counts = nullptr, total = 0;
-  cudaError_t e = cudaMalloc((void **)&counts, ((size_t)nblk + 1) * 4);
+  const int floor = d->floor_rows ? 1 : 0;
+  uint32_t *counts = nullptr, total[2] = {0u, 0u};
+  cudaError_t e = cudaMalloc((void **)&counts, (2 * (size_t)nblk + 2) * 4);
   if (e != cudaSuccess) return cuda_status(e, "pw_domain_create edge list");
-  edge_count_kernel<<<nblk, kEdgeBlock, 0, d->stream>>>(d->flags, d->special, d->nx, d->ny, d->nz, cells, counts);
-  edge_scan_kernel<<<1, kEdgeBlock, 0, d->stream>>>(counts, nblk, counts + nblk);
-  e = cudaMemcpyAsync(&total, counts + nblk, 4, cudaMemcpyDeviceToHost, d->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(d->stream);
-  if (e == cudaSuccess) e = a.alloc((void **)&d->edges, (size_t)total * 4);
-  if (e == cudaSuccess) {
-    edge_write_kernel<<<nblk, kEdgeBlock, 0, d->stream>>>(d->flags, d->special, d->nx, d->ny, d->nz, cells, counts,
-                                                          d->edges);
-    e = cudaStreamSynchronize(d->stream);
+  for (int part = 0; part <= floor; part++) {
+    uint32_t *c = counts + (size_t)part * (nblk + 1);
+    edge_count_kernel<<<nblk, kEdgeBlock, 0, d->stream>>>(d->flags, d->special, d->nx, d->ny, d->nz, cells, floor,
+                                                          part, c);
+    edge_scan_kernel<<<1, kEdgeBlock, 0, d->stream>>>(c, nblk, c + nblk);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&total[part], c + nblk, 4, cudaMemcpyDeviceToHost, d->stream);
   }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(d->stream);
+  if (e == cudaSuccess) e = a.alloc((void **)&d->edges, ((size_t)total[0] + total[1]) * 4);
+  for (int part = 0; part <= floor && e == cudaSuccess; part++)
+    edge_write_kernel<<<nblk, kEdgeBlock, 0, d->stream>>>(d->flags, d->special, d->nx, d->ny, d->nz, cells, floor,
+                                                          part, counts + (size_t)part * (nblk + 1),
+                                                          d->edges + (part ? total[0] : 0u));
+  if (e == cudaSuccess) e = cudaStreamSynchronize(d->stream);
   cudaFree(counts);
   if (e != cudaSuccess) return cuda_status(e, "pw_domain_create edge list");
-  d->edge_count = total;
-  d->nblocks = total ? (total + pw::kBlockX * pw::kBlockY - 1) / (pw::kBlockX * pw::kBlockY) : 1;
+  d->edge_count = total[0] + total[1];
+  d->edge_own = total[0];
+  d->nblocks = d->edge_count ? (d->edge_count + pw::kBlockX * pw::kBlockY - 1) / (pw::kBlockX * pw::kBlockY) : 1;
   d->plain_grid = d->nx >= 3 ? d->grid : dim3(0, 0, 0);
   return PW_OK;
 }
@@ -847,7 +862,7 @@ int pw_profile_steps(pw_domain *d, uint64_t count, float kernel_ms[3]) {
       const bool odd = (step & 1) != 0;
       if (d->split) {
         pwfast::launch_step_split(p, d->desc.storage, d->desc.op, d->desc.les, odd, d->plain_grid, d->edges,
-                                  d->edge_count, d->stream, ev[b]);
+                                  d->edge_own, d->stream, ev[b]);
       } else {
         cudaEventRecord(ev[b][0], d->stream);
         enqueue_step(d, step, ramp_speed(d, step), 0);
