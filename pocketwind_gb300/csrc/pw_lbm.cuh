@@ -1102,15 +1102,37 @@ __device__ __forceinline__ float2 raw_of_word(uint32_t w) {
 // The update and stores of a cell pair whose 19 direction values (both cells,
 // stored units) are in g: collision, rounding, the stores, the outlet's
 // upstream plane and the macros.
+// The periodic wrap of an odd step's pulls on a seam row (y = 0 or ny - 1,
+// z = 0 or nz - 1), in bytes per direction: the pull from y - 1 on y = 0
+// lands ny rows further on, the one from y + 1 on y = ny - 1 ny rows back,
+// and the same with planes in z.  The same for every cell of a row; zero off
+// the seams.  The store of direction j goes where direction opp(j) was loaded,
+// so it takes opp(j)'s correction.
+struct SeamWrap {
+  int64_t y_lo = 0, y_hi = 0, z_lo = 0, z_hi = 0;
+  __device__ __forceinline__ SeamWrap() {}
+  __device__ __forceinline__ SeamWrap(const StepParams &p, uint32_t y, uint32_t z, int64_t esize) {
+    const int64_t rows = (int64_t)p.nx * p.ny, planes = rows * p.nz;
+    y_lo = y == 0u ? rows * esize : 0;
+    y_hi = y + 1u == p.ny ? -rows * esize : 0;
+    z_lo = z == 0u ? planes * esize : 0;
+    z_hi = z + 1u == p.nz ? -planes * esize : 0;
+  }
+  __device__ __forceinline__ int64_t of(int i) const {
+    return (cy_of(i) > 0 ? y_lo : (cy_of(i) < 0 ? y_hi : 0)) + (cz_of(i) > 0 ? z_lo : (cz_of(i) < 0 ? z_hi : 0));
+  }
+};
+
 // A cell pair's inputs read again (the floor cells' rare fallback); the pair's
 // slots are not written before its stores, so a second read returns them.
 struct NoReload {
   __device__ __forceinline__ void operator()(float2 *) const {}
 };
 
-template <int ST, int OP, bool LES, bool ODD, bool FLOOR = false, class Reload = NoReload>
+template <int ST, int OP, bool LES, bool ODD, bool FLOOR = false, bool SEAM = false, class Reload = NoReload>
 __device__ __forceinline__ void pair_finish(const StepParams &p, uint32_t n, uint32_t x, uint32_t y, uint32_t z,
-                                            uint32_t ok, uint32_t eq, float2 *g, const Reload &reload = Reload()) {
+                                            uint32_t ok, uint32_t eq, float2 *g, const Reload &reload = Reload(),
+                                            const SeamWrap &sw = SeamWrap()) {
   using S = Store<ST>;
   float2 eux = f2(p.u_in), euy = f2(0.f), euz = f2(0.f);
   if ((eq & 2u) && x + 2u == p.nx) {  // the outlet is the pair's second cell (x even, nx even)
@@ -1171,7 +1193,7 @@ __device__ __forceinline__ void pair_finish(const StepParams &p, uint32_t n, uin
     // both cells stored here (nearly every pair): one branch for all directions
 #pragma unroll
     for (int j = 0; j < 19; j++) {
-      char *a = obase + p.stb[j];
+      char *a = obase + p.stb[j] + (SEAM ? sw.of(opp_of(j)) : 0);
       if (ODD && cx_of(j) != 0) {
         st_half(a, w[j] & 0xffffu);
         st_half(a + 2, w[j] >> 16);
@@ -1182,7 +1204,7 @@ __device__ __forceinline__ void pair_finish(const StepParams &p, uint32_t n, uin
   } else {
 #pragma unroll
     for (int j = 0; j < 19; j++) {
-      char *a = obase + p.stb[j];
+      char *a = obase + p.stb[j] + (SEAM ? sw.of(opp_of(j)) : 0);
       if (ODD && cx_of(j) != 0) {
         if (ok & 1u) st_half(a + (cx_of(j) < 0 ? wrap_lo : 0), w[j] & 0xffffu);
         if (ok & 2u) st_half(a + 2 + (cx_of(j) > 0 ? wrap_hi : 0), w[j] >> 16);
@@ -1216,17 +1238,18 @@ __host__ __device__ constexpr bool shifted_read(int i) {
 // A cell pair of the one-shot cell-pair kernels, its codes loaded straight
 // from HBM.  FLOOR: both cells are floor cells, whose five floor links read
 // the slots that nobody rewrites this step (halfway bounce-back).
-template <int ST, int OP, bool LES, bool ODD, bool FLOOR = false>
+template <int ST, int OP, bool LES, bool ODD, bool FLOOR = false, bool SEAM = false>
 __device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint32_t x, uint32_t y, uint32_t z,
                                            uint32_t ok, uint32_t eq) {
   // one 64-bit base per thread; each direction adds its byte offset from the
-  // kernel parameters
+  // kernel parameters (and on a seam row its wrap)
   const char *base = reinterpret_cast<const char *>(p.f) + 2 * (size_t)n;
+  const SeamWrap sw = SEAM ? SeamWrap(p, y, z, 2) : SeamWrap();
   const auto load = [&](float2 *v) {
 #pragma unroll
     for (int i = 0; i < 19; i++) {
       const bool link = FLOOR && cz_of(i) == 1;
-      const char *a = base + (link ? p.wb[i] : p.ldb[i]);
+      const char *a = base + (link ? p.wb[i] : p.ldb[i]) + (SEAM ? sw.of(i) : 0);
       if (link ? shifted_read<ODD, true>(i) : shifted_read<ODD, false>(i)) {
         v[i] = make_float2(raw_of_bits<ST>(ld_half(a)), raw_of_bits<ST>(ld_half(a + 2)));
       } else {
@@ -1236,7 +1259,7 @@ __device__ __forceinline__ void pair_cells(const StepParams &p, uint32_t n, uint
   };
   float2 g[19];
   load(g);
-  pair_finish<ST, OP, LES, ODD, FLOOR>(p, n, x, y, z, ok, eq, g, load);
+  pair_finish<ST, OP, LES, ODD, FLOOR, SEAM>(p, n, x, y, z, ok, eq, g, load, sw);
 }
 
 // The floor layer of a domain with floor rows (is_floor_cell): the z = 1 rows
@@ -1323,6 +1346,41 @@ __device__ __forceinline__ void seam_thread(const StepParams &p, uint32_t x, uin
 template <int ST, int OP, bool LES>
 __global__ void __launch_bounds__(BX) aa_step_seam(StepParams p) {
   seam_thread<ST, OP, LES>(p, blockIdx.x * BX + threadIdx.x, blockIdx.y);
+}
+
+// Odd steps on the seam rows with periodic y and z faces, as cell pairs (16-bit
+// storage, nx even): the rows of seam_thread, four per block, each direction
+// pulled and pushed across the wrap by its row's SeamWrap correction.
+template <int ST, int OP, bool LES>
+__global__ void __launch_bounds__(NTHREADS, 5) aa_step_seam_pairs(StepParams p) {
+  uint32_t r = blockIdx.y * BY + threadIdx.y;
+  if (r >= seam_rows(p.ny, p.nz)) return;
+  const uint32_t zs = p.nz > 1u ? 2u : 1u, ys = p.ny > 1u ? 2u : 1u;
+  uint32_t y, z;
+  if (r < zs * p.ny) {
+    z = r < p.ny ? 0u : p.nz - 1u;
+    y = r < p.ny ? r : r - p.ny;
+  } else {
+    r -= zs * p.ny;
+    z = 1u + r / ys;
+    y = (r % ys) ? p.ny - 1u : 0u;
+  }
+  const uint32_t x = blockIdx.x * (2 * BX) + 2u * threadIdx.x;
+  if (x >= p.nx) return;
+  const uint32_t n = x + p.nx * (y + p.ny * z);
+  const uint32_t word = __ldg(&p.special[n >> 5]);
+  uint32_t ok = 0u, eq = 0u;
+#pragma unroll
+  for (uint32_t k = 0; k < 2u; k++) {
+    const uint32_t xk = x + k, nk = n + k;
+    if (!((word >> (nk & 31u)) & 1u)) {
+      if (is_plain_position(xk, p.nx)) ok |= 1u << k;
+    } else if (__ldg(&p.flags[nk]) == EQ) {
+      ok |= 1u << k;
+      eq |= 1u << k;
+    }
+  }
+  if (ok) pair_cells<ST, OP, LES, true, false, true>(p, n, x, y, z, ok, eq);
 }
 
 __device__ __forceinline__ void cell_coords(const StepParams &p, uint32_t n, uint32_t &x, uint32_t &y, uint32_t &z) {
@@ -1719,6 +1777,21 @@ void launch_step(const StepParams &p, int storage, int op, int les, bool odd, di
 static inline void mark(const cudaEvent_t *ev, int k, cudaStream_t s) {
   if (ev) cudaEventRecord(ev[k], s);
 }
+// The seam rows of an odd step: as cell pairs with periodic faces (16-bit
+// storage, nx even), else one cell per thread (free-slip faces reflect).
+template <int ST, int OP, bool LES>
+static void launch_seam(const StepParams &p, dim3 g, cudaStream_t s) {
+  const uint32_t rows = seam_rows(p.ny, p.nz);
+  if constexpr (ST != STORE_F32) {
+    if ((p.nx & 1u) == 0u && p.slip == 0u) {
+      const dim3 grid((p.nx + 2 * BX - 1) / (2 * BX), (rows + BY - 1) / BY);
+      aa_step_seam_pairs<ST, OP, LES><<<grid, dim3(BX, BY), 0, s>>>(p);
+      return;
+    }
+  }
+  aa_step_seam<ST, OP, LES><<<dim3(g.x, rows), BX, 0, s>>>(p);
+}
+
 // The floor layer's kernel, when the domain's floor rows are on (16-bit
 // storage with nx even only: the floor rows are decided at domain creation).
 template <int ST, int OP, bool LES>
@@ -1745,7 +1818,7 @@ static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *l
   }
   if (side) {
     // launched first so their few blocks start before the plain grid fills the GPU
-    if (plain && odd) aa_step_seam<ST, OP, LES><<<dim3(g.x, seam_rows(p.ny, p.nz)), BX, 0, t>>>(p);
+    if (plain && odd) launch_seam<ST, OP, LES>(p, g, t);
     launch_floor<ST, OP, LES>(p, odd, t);
     if (count) {
       unsigned blocks = (count + NTHREADS - 1) / NTHREADS;
@@ -1770,7 +1843,7 @@ static void step_split3(const StepParams &p, bool odd, dim3 g, const uint32_t *l
       }
       mark(ev, 1, s);
       mark(ev, 2, s);
-      if (!side) aa_step_seam<ST, OP, LES><<<dim3(g.x, seam_rows(p.ny, p.nz)), BX, 0, s>>>(p);
+      if (!side) launch_seam<ST, OP, LES>(p, g, s);
       mark(ev, 3, s);
     } else {
       mark(ev, 0, s);
