@@ -7,7 +7,9 @@
 //   plain  R rows x 64 cells of one member (two cells per thread: the 32-bit
 //          cell-pair kernel for 16-bit storage, x / x + 32 else;
 //          even steps every row, odd steps the rows off the y/z seams);
-//   seam   4 seam rows x 32 cells (odd steps; seam_thread);
+//   seam   4 seam rows x 64 cells as cell pairs with periodic wrap corrections
+//          (odd steps, 16-bit storage, every nx even, periodic faces;
+//          seam_pair_thread), else 4 rows x 32 cells one per thread (seam_thread);
 //   edge   128 listed cells (edge_block), whose force partial goes to the
 //          member's slot of that block, exactly as its own edge kernel does.
 // A step is two persistent launches, as a single domain's step is: the plain
@@ -82,10 +84,22 @@ __global__ void __launch_bounds__(kBatchThreads, PLAIN ? 6 : 1) batch_step(const
           pwbatch::plain_thread<ST, OP, LES, ODD>(sp, run * 64u + (tid & 31u), yr + off, zb + off);
       }
     } else if (kind == 1) {
-      const uint32_t runs = (sp.nx + 31u) / 32u;
-      const uint32_t run = local % runs, g = local / runs;
-      const uint32_t row = g * (kBatchThreads / 32) + (tid >> 5);
-      if (row < pwbatch::seam_rows(sp.ny, sp.nz)) pwbatch::seam_thread<ST, OP, LES>(sp, run * 32u + (tid & 31u), row);
+      bool paired = false;
+      if constexpr (PAIRS && ST != pw::STORE_F32) {
+        if (sp.slip == 0u) {  // cell pairs with periodic wrap corrections
+          paired = true;
+          const uint32_t runs = (sp.nx + 63u) / 64u;
+          const uint32_t run = local % runs, g = local / runs;
+          pwbatch::seam_pair_thread<ST, OP, LES>(sp, run * 64u + 2u * (tid & 31u),
+                                                 g * (kBatchThreads / 32) + (tid >> 5));
+        }
+      }
+      if (!paired) {
+        const uint32_t runs = (sp.nx + 31u) / 32u;
+        const uint32_t run = local % runs, g = local / runs;
+        const uint32_t row = g * (kBatchThreads / 32) + (tid >> 5);
+        if (row < pwbatch::seam_rows(sp.ny, sp.nz)) pwbatch::seam_thread<ST, OP, LES>(sp, run * 32u + (tid & 31u), row);
+      }
     } else {
       pwbatch::edge_block<ST, OP, LES, ODD>(sp, lists[m], counts[m], local, tid);
     }
@@ -106,6 +120,9 @@ void launch3(bool odd, bool plain, bool pairs, unsigned blocks, cudaStream_t s, 
       if (odd) PW_BATCH_LAUNCH(true, true, false);
       else PW_BATCH_LAUNCH(false, true, false);
     }
+  } else if (pairs && ST != pw::STORE_F32) {
+    if (odd) PW_BATCH_LAUNCH(true, false, true);
+    else PW_BATCH_LAUNCH(false, false, true);
   } else {
     if (odd) PW_BATCH_LAUNCH(true, false, false);
     else PW_BATCH_LAUNCH(false, false, false);
@@ -172,7 +189,12 @@ int build_segments(pw_batch *b) {
       const uint32_t runs = (v.nx + 63u) / 64u;
       const uint32_t nyr = v.ny > 2u * off ? v.ny - 2u * off : 0u, nzr = v.nz > 2u * off ? v.nz - 2u * off : 0u;
       const uint32_t plain = v.nx >= 3u ? runs * ((nyr + b->rows - 1u) / b->rows) * nzr : 0u;
-      const uint32_t seam = par && v.nx >= 3u ? ((v.nx + 31u) / 32u) * ((pwbatch::seam_rows(v.ny, v.nz) + 3u) / 4u) : 0u;
+      // seam items: 4 rows of 64 cells as cell pairs (16-bit storage, nx even,
+      // periodic faces), else of 32 cells one per thread
+      const bool paired = b->pairs && v.storage != pw::STORE_F32 && v.slip == 0u;
+      const uint32_t seam_run = paired ? 64u : 32u;
+      const uint32_t seam =
+          par && v.nx >= 3u ? ((v.nx + seam_run - 1u) / seam_run) * ((pwbatch::seam_rows(v.ny, v.nz) + 3u) / 4u) : 0u;
       const uint32_t edge = (v.edge_count + kBatchThreads - 1u) / kBatchThreads;
       const uint32_t kinds[3] = {plain, seam, edge};
       for (uint32_t k = 0; k < 3; k++) {

@@ -917,6 +917,7 @@ MemberView member_view(const pw_domain *d) {
   v.interpolated = d->interp;
   v.edges = d->edges;
   v.edge_count = d->edge_count;
+  v.slip = d->slip;
   v.status = d->status_dev;
   v.stream = d->stream;
   return v;

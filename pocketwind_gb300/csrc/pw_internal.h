@@ -49,6 +49,7 @@ struct MemberView {
   uint64_t steps;
   bool ramping;              // inlet ramp still in progress
   bool interpolated;         // interpolated (Bouzidi) walls
+  uint32_t slip;             // free-slip faces (bit 0 y, bit 1 z)
   const uint32_t *edges;
   uint32_t edge_count;
   uint32_t *status;

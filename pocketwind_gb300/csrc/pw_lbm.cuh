@@ -1352,9 +1352,8 @@ __global__ void __launch_bounds__(BX) aa_step_seam(StepParams p) {
 // storage, nx even): the rows of seam_thread, four per block, each direction
 // pulled and pushed across the wrap by its row's SeamWrap correction.
 template <int ST, int OP, bool LES>
-__global__ void __launch_bounds__(NTHREADS, 5) aa_step_seam_pairs(StepParams p) {
-  uint32_t r = blockIdx.y * BY + threadIdx.y;
-  if (r >= seam_rows(p.ny, p.nz)) return;
+__device__ __forceinline__ void seam_pair_thread(const StepParams &p, uint32_t x, uint32_t r) {
+  if (r >= seam_rows(p.ny, p.nz) || x >= p.nx) return;
   const uint32_t zs = p.nz > 1u ? 2u : 1u, ys = p.ny > 1u ? 2u : 1u;
   uint32_t y, z;
   if (r < zs * p.ny) {
@@ -1365,8 +1364,6 @@ __global__ void __launch_bounds__(NTHREADS, 5) aa_step_seam_pairs(StepParams p) 
     z = 1u + r / ys;
     y = (r % ys) ? p.ny - 1u : 0u;
   }
-  const uint32_t x = blockIdx.x * (2 * BX) + 2u * threadIdx.x;
-  if (x >= p.nx) return;
   const uint32_t n = x + p.nx * (y + p.ny * z);
   const uint32_t word = __ldg(&p.special[n >> 5]);
   uint32_t ok = 0u, eq = 0u;
@@ -1381,6 +1378,11 @@ __global__ void __launch_bounds__(NTHREADS, 5) aa_step_seam_pairs(StepParams p) 
     }
   }
   if (ok) pair_cells<ST, OP, LES, true, false, true>(p, n, x, y, z, ok, eq);
+}
+
+template <int ST, int OP, bool LES>
+__global__ void __launch_bounds__(NTHREADS, 5) aa_step_seam_pairs(StepParams p) {
+  seam_pair_thread<ST, OP, LES>(p, blockIdx.x * (2 * BX) + 2u * threadIdx.x, blockIdx.y * BY + threadIdx.y);
 }
 
 __device__ __forceinline__ void cell_coords(const StepParams &p, uint32_t n, uint32_t &x, uint32_t &y, uint32_t &z) {
