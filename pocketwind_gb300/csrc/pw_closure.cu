@@ -291,7 +291,7 @@ __device__ __forceinline__ void cell_inputs(const StepParams &p, const float *st
 // rounding, stores, macros and outlet plane, as general_cell ends.
 template <int ST, bool ODD>
 __device__ __forceinline__ void finish_plain_reg(const StepParams &p, uint32_t x, uint32_t y, uint32_t z, uint32_t n,
-                                                 const float *st, float c, float *post) {
+                                                 const float *st, float c, float *post, bool interior) {
   using S = pw::Store<ST>;
   using T = typename S::T;
   const float tau_s = st[0];
@@ -315,12 +315,17 @@ __device__ __forceinline__ void finish_plain_reg(const StepParams &p, uint32_t x
   const float rho = st[1];
   if (p.write_macro && !(rho >= 0.5f && rho <= 1.5f)) atomicOr(p.status, 1u);  // also catches NaN
   T *f = reinterpret_cast<T *>(p.f);
-  const pwclosure::Nbr b = pwclosure::make_nbr(p, x, y, z);
   T code[19];
 #pragma unroll
   for (int j = 0; j < 19; j++) code[j] = S::encode(post[j], (uint32_t)j, n);
+  if (interior) {
 #pragma unroll
-  for (int j = 0; j < 19; j++) f[ODD ? b.push(j, p.stride) : (pw::pidx)pw::opp_of(j) * p.stride + n] = code[j];
+    for (int j = 0; j < 19; j++) f[n + p.st[j]] = code[j];
+  } else {
+    const pwclosure::Nbr b = pwclosure::make_nbr(p, x, y, z);
+#pragma unroll
+    for (int j = 0; j < 19; j++) f[ODD ? b.push(j, p.stride) : (pw::pidx)pw::opp_of(j) * p.stride + n] = code[j];
+  }
   if (p.write_macro) p.macros[n] = make_float4(rho, st[2], st[3], st[4]);
   if (x + 2 == p.nx) p.plane_out[y + p.ny * z] = pwclosure::outlet_velocity_of<ST>(code);
 }
@@ -350,12 +355,21 @@ __global__ void __launch_bounds__(128, 4) closure_step(StepParams p, const uint3
 #pragma unroll
     for (int k = 0; k < kIn; k++) xin[k] = 0.0f;
     const bool plain = in && flag == pw::FLUID;  // fluid without wall links
+    // cells whose neighbours need no periodic wrap take the step's element
+    // offsets from the kernel parameters (the wrap arithmetic otherwise)
+    const bool interior = x >= 1u && x + 2u <= p.nx && y >= 1u && y + 2u <= p.ny && z >= 1u && z + 2u <= p.nz &&
+                          p.slip == 0u;
     if (plain) {
       const T *f = reinterpret_cast<const T *>(p.f);
-      const pwclosure::Nbr b = pwclosure::make_nbr(p, x, y, z);
       float g[19];
+      if (interior) {
 #pragma unroll
-      for (int i = 0; i < 19; i++) g[i] = S::decode(f[ODD ? b.pull(i, p.stride) : (pw::pidx)i * p.stride + n]);
+        for (int i = 0; i < 19; i++) g[i] = S::decode(f[n + p.ld[i]]);
+      } else {
+        const pwclosure::Nbr b = pwclosure::make_nbr(p, x, y, z);
+#pragma unroll
+        for (int i = 0; i < 19; i++) g[i] = S::decode(f[ODD ? b.pull(i, p.stride) : (pw::pidx)i * p.stride + n]);
+      }
       float rho, vx, vy, vz;
       pwclosure::update_fast<OP, true, CaptureHook>(p, g, rho, vx, vy, vz, 1.0f, 1.0f, CaptureHook{st});
       cell_inputs(p, st, (float)wall_dist[n], xin);
@@ -372,7 +386,7 @@ __global__ void __launch_bounds__(128, 4) closure_step(StepParams p, const uint3
       float post[19];
 #pragma unroll
       for (int i = 0; i < 19; i++) post[i] = post_s[OP == pw::OP_REG ? i : 0][tid];
-      finish_plain_reg<ST, ODD>(p, x, y, z, n, st, c, post);
+      finish_plain_reg<ST, ODD>(p, x, y, z, n, st, c, post, interior);
     } else if (in) {
       pwclosure::general_cell<ST, OP, true, ODD, ClosureHook>(p, x, y, z, n, flag, fx, fy, fz, any, ClosureHook{c});
     }
