@@ -148,3 +148,38 @@ def test_batch_refuses_mixed_or_misused_members():
     with pytest.raises(solver.RangeError):
         batch.step(1)
     batch.destroy()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["f16", "bf16"])
+def test_floor_kernel_matches_the_general_path(precision):
+    """A domain with a floor stepped alone runs its first fluid layer in the
+    floor kernel (the LES wall cell of stream_collide.wgsl:18-80 in closed form
+    for a flat floor); the same domain stepped in a batch takes those cells
+    through the one-cell general path, which evaluates the wall cell in the
+    reference's own order.  After 40 steps of the 64x32x32 vehicle (REG + LES
+    + wall model) the two agree to the 16-bit storage's rounding (the bound of
+    the batch's 16-bit comparison above), with the floor layer itself compared
+    on its own."""
+    from pocketwind_gb300 import solver
+    from pocketwind_gb300.batch import Batch
+    case = cases.vehicle_case(64)
+    grid = case.grid()
+    alone = solver.GpuSolver.create(case.layout, grid, case.params(precision))
+    member = solver.GpuSolver.create(case.layout, grid, case.params(precision))
+    batch = Batch([member])
+    alone.step(40, True)
+    batch.step(40, True)
+    a, b = alone.macros().astype(np.float64), member.macros().astype(np.float64)
+    nx, ny, nz = case.layout
+    z = np.arange(nx * ny * nz) // (nx * ny)
+    floor_layer = (z == 1) & ((grid.flags & 7) == 0)
+    assert floor_layer.sum() > 0
+    tol = 2e-3 if precision == "f16" else 1e-2  # bfloat16 keeps 8 bits
+    for cells in (floor_layer, (grid.flags & 7) == 0):
+        assert _l2_err(a[cells, 1:], b[cells, 1:]) < tol, cells.sum()
+    alone.encode_force()
+    member.encode_force()
+    fa, fb = alone.read_force(), member.read_force()
+    assert abs(fa.fx - fb.fx) <= tol * abs(fb.fx)
+    batch.destroy()
