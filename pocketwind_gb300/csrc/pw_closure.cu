@@ -108,20 +108,16 @@ __device__ __forceinline__ void tc_commit(uint64_t *bar) {
 }
 __device__ __forceinline__ void tc_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-// 32 binary32 columns from col of this thread's TMEM lane (warp w reads lanes 32w..32w+31).
-__device__ __forceinline__ void tc_load32(uint32_t taddr, float *v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
-      "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
+// 8 binary32 columns from column col of this thread's TMEM lane (warp w reads
+// lanes 32w..32w+31), waited for.
+__device__ __forceinline__ void tc_load8(uint32_t taddr, float *v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int j = 0; j < 32; j++) v[j] = __uint_as_float(r[j]);
+  for (int j = 0; j < 8; j++) v[j] = __uint_as_float(r[j]);
 }
 
 // Shared state of a block's network evaluation.
@@ -204,26 +200,26 @@ __device__ float block_mlp(TcShared &sh, const float x[kIn], uint32_t &phase) {
     tc_mma(sh.tmem, smem_desc(smem_u32(sh.a1), kSbo1), smem_desc(smem_u32(sh.img + kImgW1), kSbo1), 0u);
     tc_commit(&sh.bar);
   }
-  float h[32];
   // each warp reads TMEM only when all its lanes saw the layer complete
   const bool done1 = __all_sync(0xffffffffu, live && tc_wait(&sh.bar, phase & 1u));
   phase++;
   tc_after_sync();
-  if (done1) {
-    tc_load32(lane_addr, h);
-  } else {
-    if (live) atomicOr(&sh.failed, 1u);
-#pragma unroll
-    for (int k = 0; k < 32; k++) h[k] = 0.0f;
-  }
+  if (!done1 && live) atomicOr(&sh.failed, 1u);
   const float *b1 = reinterpret_cast<const float *>(sh.img + kImgB1);
 #pragma unroll
-  for (int k = 0; k < 32; k += 8) {
+  for (int k = 0; k < 32; k += 8) {  // eight columns at a time: fewer live registers
+    float h[8];
+    if (done1) {
+      tc_load8(lane_addr + (uint32_t)k, h);
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; j++) h[j] = 0.0f;
+    }
     uint4 v;
-    v.x = pack_bf16(tanh_fast(h[k] + b1[k]), tanh_fast(h[k + 1] + b1[k + 1]));
-    v.y = pack_bf16(tanh_fast(h[k + 2] + b1[k + 2]), tanh_fast(h[k + 3] + b1[k + 3]));
-    v.z = pack_bf16(tanh_fast(h[k + 4] + b1[k + 4]), tanh_fast(h[k + 5] + b1[k + 5]));
-    v.w = pack_bf16(tanh_fast(h[k + 6] + b1[k + 6]), tanh_fast(h[k + 7] + b1[k + 7]));
+    v.x = pack_bf16(tanh_fast(h[0] + b1[k]), tanh_fast(h[1] + b1[k + 1]));
+    v.y = pack_bf16(tanh_fast(h[2] + b1[k + 2]), tanh_fast(h[3] + b1[k + 3]));
+    v.z = pack_bf16(tanh_fast(h[4] + b1[k + 4]), tanh_fast(h[5] + b1[k + 5]));
+    v.w = pack_bf16(tanh_fast(h[6] + b1[k + 6]), tanh_fast(h[7] + b1[k + 7]));
     *reinterpret_cast<uint4 *>(sh.a2 + cm_offset(tid, k, kSbo2)) = v;
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -244,12 +240,16 @@ __device__ float block_mlp(TcShared &sh, const float x[kIn], uint32_t &phase) {
     if (live2) atomicOr(&sh.failed, 1u);
     return 0.0f;
   }
-  tc_load32(lane_addr + 32u, h);
   const float *b2 = reinterpret_cast<const float *>(sh.img + kImgB2);
   const float *w3 = reinterpret_cast<const float *>(sh.img + kImgW3);
   float out = 0.0f;
 #pragma unroll
-  for (int k = 0; k < 32; k++) out = fmaf(w3[k], bf16_round(tanh_fast(h[k] + b2[k])), out);
+  for (int k = 0; k < 32; k += 8) {
+    float h[8];
+    tc_load8(lane_addr + 32u + (uint32_t)k, h);
+#pragma unroll
+    for (int j = 0; j < 8; j++) out = fmaf(w3[k + j], bf16_round(tanh_fast(h[j] + b2[k + j])), out);
+  }
   return out + reinterpret_cast<const float *>(sh.img + kImgB3)[0];
 }
 
