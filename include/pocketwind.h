@@ -227,7 +227,8 @@ PW_API int pw_read_totals(pw_domain *dom, double out[4]);
 /* The density guard (src/lbm/nan-guard.ts:39,151-196, nan_guard.wgsl): the
  * stream-collide pass flags any fluid cell whose density is non-finite or
  * outside [0.5, 1.5] on steps that write macros.  Returns the flag of the
- * latest macro step in *unstable. */
+ * latest macro step in *unstable, and PW_ERR_TIMEOUT when a staged-row step
+ * (PW_KERNEL_TILE) gave up waiting for its copies since that step. */
 PW_API int pw_guard_check(pw_domain *dom, int *unstable);
 /* injectNaNForRunner (gpu-solver.ts:358-375): a quiet NaN into the rest
  * population of the first fluid cell, written from the host. */

@@ -821,6 +821,10 @@ int pw_guard_check(pw_domain *d, int *unstable) {
   PW_TRY(cudaMemcpyAsync(d->status_host, d->status_dev, 4, cudaMemcpyDeviceToHost, d->stream));
   PW_TRY(cudaStreamSynchronize(d->stream));
   *unstable = (d->status_host[0] & 1u) ? 1 : 0;
+  if (d->status_host[0] & 2u) {
+    set_error("A step's staged copies did not complete in time (the step's state is not valid).");
+    return PW_ERR_TIMEOUT;
+  }
   return PW_OK;
 }
 
