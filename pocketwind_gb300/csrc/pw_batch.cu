@@ -1,6 +1,6 @@
-// Batched stepping of many independent domains: one persistent launch per step
-// over the work of every member, replayed from captured CUDA graphs, with the
-// launch shape chosen by timing (pw_batch_tune).  No counterpart in the
+// Batched stepping of many independent domains: two concurrent persistent
+// launches per step over the work of every member, replayed from captured CUDA
+// graphs, with the launch shape chosen by timing (pw_batch_tune).  No counterpart in the
 // reference, which runs one solver at a time (src/app/solver-slot.ts).
 //
 // Work items (per step parity):
@@ -47,10 +47,15 @@ constexpr int kChunk = 50;                        // steps per captured graph
 // PLAIN: the plain items (PAIRS: through the 32-bit cell-pair kernel, which
 // needs 16-bit storage and every member's nx even); otherwise
 // the seam and edge items.
-// The plain kernels are held to 85 registers (6 blocks per SM): the member's
+// The plain kernels are held to 72 registers (7 blocks per SM): the member's
 // offset tables sit in shared memory and are reloaded rather than kept live.
+// Measured on the 64-tunnel batch: 6 blocks (85 registers) 0.8% slower, 8
+// blocks (64 registers, 140 bytes spilled per thread) 4% slower.
+#ifndef PW_BATCH_PLAIN_BLOCKS
+#define PW_BATCH_PLAIN_BLOCKS 7
+#endif
 template <int ST, int OP, bool LES, bool ODD, bool PLAIN, bool PAIRS>
-__global__ void __launch_bounds__(kBatchThreads, PLAIN ? 6 : 1) batch_step(const StepParams *params, const BatchSeg *segs,
+__global__ void __launch_bounds__(kBatchThreads, PLAIN ? PW_BATCH_PLAIN_BLOCKS : 1) batch_step(const StepParams *params, const BatchSeg *segs,
                                                              const uint32_t *item_seg, uint32_t total,
                                                              const uint32_t *const *lists, const uint32_t *counts,
                                                              uint32_t rows) {

@@ -80,17 +80,18 @@ __device__ __forceinline__ uint32_t lowbias32(uint32_t bits, uint32_t i, uint32_
 __host__ __device__ constexpr uint32_t dither_mul(int i) { return (0x9e3779b1u ^ ((uint32_t)i * 0x85ebca6bu)) | 1u; }
 
 // Random bits for encode_pair of two codes of direction i: for each value the
-// top bits of its own hash bits * dither_mul(i) + nk (nk = n * 0x9e3779b9 of
-// its cell), the best-mixed bits of a multiplicative hash and the ones
-// encode_fast uses, so a code's rounding depends on its own value, cell and
-// direction only, never on its partner's.  f16 takes 13 bits per half (h >> 19
-// into bits 12:0 and 28:16), bfloat16 16 (h >> 16 into each half).
+// upper half of its own hash bits * dither_mul(i) + nk (nk = n * 0x9e3779b9
+// of its cell), so a code's rounding depends on its own value, cell and
+// direction only, never on its partner's.  One byte permute puts h_lo[31:16]
+// in the low half and h_hi[31:16] in the high half: bfloat16 adds all 16 bits
+// of each half, f16 the 13 bits 12:0 and 28:16, that is hash bits 28:16 (the
+// one-code encode_fast takes bits 31:19 of the same hash: the same rounding
+// probabilities, another realization).
 template <int ST>
 __device__ __forceinline__ uint32_t pair_dither(float hi, float lo, uint32_t mj, uint32_t nk_hi, uint32_t nk_lo) {
   const uint32_t h_hi = __float_as_uint(hi) * mj + nk_hi;
   const uint32_t h_lo = __float_as_uint(lo) * mj + nk_lo;
-  if (ST == STORE_F16) return ((h_hi >> 3) & 0x1fff0000u) | (h_lo >> 19);
-  return __byte_perm(h_lo, h_hi, 0x7632u);  // h_lo[31:16] low, h_hi[31:16] high
+  return __byte_perm(h_lo, h_hi, 0x7632u);
 }
 
 template <int S> struct Store;
