@@ -365,6 +365,10 @@ int pw_batch_create(pw_domain *const *members, uint32_t count, pw_batch **out) {
       set_error("Batch members must use the fast build's one-cell-per-thread kernels (strict = 0, kernel AUTO/CELL).");
       return PW_ERR_INVALID;
     }
+    if (v.closure) {
+      set_error("Batch members cannot have a learned closure attached.");
+      return PW_ERR_INVALID;
+    }
     if (v.storage != first.storage || v.op != first.op || v.les != first.les) {
       set_error("Batch members must share storage, collision operator and LES.");
       return PW_ERR_INVALID;

@@ -12,17 +12,23 @@
 // within two coarse cells of a wall or of the x faces are left out (the wall
 // model owns the wall cells).
 //
-// Inference (closure_step): one cell per thread, 128 cells per block; a first
-// pass takes each plain LES cell's Smagorinsky state from its populations, its
-// strain S = -3 Pi_neq / (2 rho tau_s) and the nine inputs; the block then runs
-// the network for its 128 cells on the 5th-generation tensor cores: each layer
-// is one tcgen05.mma of M = 128 cells by N = 32 outputs (K = 16 inputs, or two
-// of K = 16 hidden units), bf16 operands in shared memory, binary32
-// accumulators in tensor memory, issued by one thread and read back by every
-// thread for its own cell (tcgen05.ld); the second pass is the ordinary cell
-// update with tau = tau0 + (tau_s - tau0) max(0, 1 + c): for the regularized
-// operator the first pass's Smagorinsky post-collision state is corrected in
-// place (finish_plain_reg), for TRT the cell goes through the one-cell path again.
+// Inference, periodic faces (closure_pairs): the plain step's two-cell update
+// (update_fast2) with a hook between the Smagorinsky relaxation time and the
+// reconstruction.  Each thread takes cells x and x + 32 of a row, a block the
+// 256 cells of four rows; the hook takes each plain LES cell's strain
+// S = -3 Pi_neq / (2 rho tau_s) and its nine inputs, and the block runs the
+// network for its cells on the 5th-generation tensor cores as two tiles of
+// M = 128 cells: each layer is one tcgen05.mma per tile of N = 32 outputs
+// (K = 16 inputs, or two of K = 16 hidden units), bf16 operands in shared
+// memory, binary32 accumulators in tensor memory, issued by one thread and
+// read back by every thread for its own cells (tcgen05.ld); the update then
+// goes on with tau = tau0 + (tau_s - tau0) max(0, 1 + c).  The wall-link cells
+// and the floor layer run in the edge and floor kernels beside it with plain
+// Smagorinsky and the reference's wall model, as in a step without the closure.
+// Free-slip faces (closure_step): one cell per thread over every cell, 128
+// cells per block, the same network on one tile; for the regularized operator
+// the first pass's Smagorinsky post-collision state is corrected in place
+// (finish_plain_reg), for TRT the cell goes through the one-cell path again.
 #define PW_NS pwclosure
 #define PW_STRICT 0
 #include <algorithm>
@@ -146,7 +152,8 @@ __device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity) {
 
 // Block start: copy the image, set up the barrier, allocate 64 TMEM columns
 // (warp 0).  All 128 threads call it.
-__device__ void tc_setup(TcShared &sh, const uint32_t *frag) {
+template <class Sh>
+__device__ void tc_setup(Sh &sh, const uint32_t *frag) {
   const uint32_t tid = threadIdx.x + 32u * threadIdx.y;
   const uint32_t *src = frag;
   uint32_t *dst = reinterpret_cast<uint32_t *>(sh.img);
@@ -167,7 +174,8 @@ __device__ void tc_setup(TcShared &sh, const uint32_t *frag) {
 }
 
 // Block end: free the TMEM columns (warp 0), after every thread's last read.
-__device__ void tc_teardown(TcShared &sh) {
+template <class Sh>
+__device__ void tc_teardown(Sh &sh) {
   tc_before_sync();
   __syncthreads();
   tc_after_sync();
@@ -393,6 +401,264 @@ __global__ void __launch_bounds__(128, 4) closure_step(StepParams p, const uint3
     // the partial slot of tile (x block, y block, z), as the cell kernels number them
     const size_t slot = tile;
     pwclosure::reduce_force_at(any, fx, fy, fz, p.partials, slot, threadIdx.x + 32 * threadIdx.y);
+  }
+  if (threadIdx.x == 0 && threadIdx.y == 0 && sh.failed) atomicOr(p.status, 4u);
+  tc_teardown(sh);
+}
+
+// ---------------------------------------------------------------- cell-pair closure step
+// The closure step on the plain step's two-cell arithmetic (update_fast2):
+// each thread takes cells x and x + 32 of a 64-cell run, as aa_step_fast does
+// for every storage, and a block the 256 cells of four rows, so its network
+// runs as two M = 128 tiles, the threads' first cells and their second cells.
+// Every row of both parities runs here, the seam rows with their periodic
+// wrap as per-row offsets (SeamWrap); the wall-link cells and the floor layer
+// run in the edge and floor kernels beside it, with the reference's wall
+// model, as in a step without the closure.
+struct TcPair {
+  __align__(128) unsigned char img[kImgBytes];   // the network image
+  // the layer-2 operands of the two tiles (128 x 32 bf16 each); the layer-1
+  // operands (128 x 16) share their first half, which layer 1's MMAs have
+  // read by the time its outputs come back
+  __align__(128) unsigned char a2[2][128 * 64];
+  __align__(8) uint64_t bar;                     // MMA completion
+  uint32_t tmem;                                 // 64 TMEM columns: tile t's layer output at column 32 t
+  uint32_t failed;                               // a completion wait ran out
+  __device__ __forceinline__ unsigned char *a1(int t) { return a2[0] + t * (128 * 32); }
+};
+
+__device__ __forceinline__ void put_inputs(unsigned char *a1, uint32_t row, const float x[kIn]) {
+  uint4 lo, hi;
+  lo.x = pack_bf16(x[0], x[1]); lo.y = pack_bf16(x[2], x[3]); lo.z = pack_bf16(x[4], x[5]);
+  lo.w = pack_bf16(x[6], x[7]);
+  hi.x = pack_bf16(x[8], 0.0f); hi.y = 0u; hi.z = 0u; hi.w = 0u;
+  *reinterpret_cast<uint4 *>(a1 + cm_offset(row, 0, kSbo1)) = lo;
+  *reinterpret_cast<uint4 *>(a1 + cm_offset(row, 8, kSbo1)) = hi;
+}
+
+// block_mlp for the block's two tiles: c of the thread's first (.x) and
+// second (.y) cell.  Layer 2 writes the columns layer 1's outputs were read
+// from, after the block barrier that follows those reads.
+__device__ float2 block_mlp2(TcPair &sh, const float xa[kIn], const float xb[kIn], uint32_t &phase) {
+  const uint32_t tid = threadIdx.x + 32u * threadIdx.y, warp = tid >> 5;
+  const uint32_t lane_addr = sh.tmem + ((warp * 32u) << 16);
+  put_inputs(sh.a1(0), tid, xa);
+  put_inputs(sh.a1(1), tid, xb);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  tc_before_sync();
+  __syncthreads();
+  tc_after_sync();
+  const bool live = sh.failed == 0u;
+  if (tid == 0 && live) {
+    const uint64_t w1 = smem_desc(smem_u32(sh.img + kImgW1), kSbo1);
+    tc_mma(sh.tmem, smem_desc(smem_u32(sh.a1(0)), kSbo1), w1, 0u);
+    tc_mma(sh.tmem + 32u, smem_desc(smem_u32(sh.a1(1)), kSbo1), w1, 0u);
+    tc_commit(&sh.bar);
+  }
+  const bool done1 = __all_sync(0xffffffffu, live && tc_wait(&sh.bar, phase & 1u));
+  phase++;
+  tc_after_sync();
+  if (!done1 && live) atomicOr(&sh.failed, 1u);
+  const float *b1 = reinterpret_cast<const float *>(sh.img + kImgB1);
+#pragma unroll
+  for (int t = 0; t < 2; t++) {
+#pragma unroll
+    for (int k = 0; k < 32; k += 8) {
+      float h[8];
+      if (done1) {
+        tc_load8(lane_addr + 32u * t + (uint32_t)k, h);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; j++) h[j] = 0.0f;
+      }
+      uint4 v;
+      v.x = pack_bf16(tanh_fast(h[0] + b1[k]), tanh_fast(h[1] + b1[k + 1]));
+      v.y = pack_bf16(tanh_fast(h[2] + b1[k + 2]), tanh_fast(h[3] + b1[k + 3]));
+      v.z = pack_bf16(tanh_fast(h[4] + b1[k + 4]), tanh_fast(h[5] + b1[k + 5]));
+      v.w = pack_bf16(tanh_fast(h[6] + b1[k + 6]), tanh_fast(h[7] + b1[k + 7]));
+      *reinterpret_cast<uint4 *>(sh.a2[t] + cm_offset(tid, k, kSbo2)) = v;
+    }
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  tc_before_sync();
+  __syncthreads();
+  tc_after_sync();
+  const bool live2 = sh.failed == 0u;
+  if (tid == 0 && live2) {
+    const uint32_t w2 = smem_u32(sh.img + kImgW2);
+#pragma unroll
+    for (int t = 0; t < 2; t++) {
+      const uint32_t a2 = smem_u32(sh.a2[t]);
+      tc_mma(sh.tmem + 32u * t, smem_desc(a2, kSbo2), smem_desc(w2, kSbo2), 0u);
+      tc_mma(sh.tmem + 32u * t, smem_desc(a2 + 2u * kLbo, kSbo2), smem_desc(w2 + 2u * kLbo, kSbo2), 1u);
+    }
+    tc_commit(&sh.bar);
+  }
+  const bool done2 = __all_sync(0xffffffffu, live2 && tc_wait(&sh.bar, phase & 1u));
+  phase++;
+  tc_after_sync();
+  if (!done2) {
+    if (live2) atomicOr(&sh.failed, 1u);
+    return make_float2(0.0f, 0.0f);
+  }
+  const float *b2 = reinterpret_cast<const float *>(sh.img + kImgB2);
+  const float *w3 = reinterpret_cast<const float *>(sh.img + kImgW3);
+  float out[2] = {0.0f, 0.0f};
+#pragma unroll
+  for (int t = 0; t < 2; t++) {
+#pragma unroll
+    for (int k = 0; k < 32; k += 8) {
+      float h[8];
+      tc_load8(lane_addr + 32u * t + (uint32_t)k, h);
+#pragma unroll
+      for (int j = 0; j < 8; j++) out[t] = fmaf(w3[k + j], bf16_round(tanh_fast(h[j] + b2[k + j])), out[t]);
+    }
+  }
+  const float b3 = reinterpret_cast<const float *>(sh.img + kImgB3)[0];
+  return make_float2(out[0] + b3, out[1] + b3);
+}
+
+// update_fast2's hook: the network's relaxation time for the lanes in live
+// (bit 0 .x, bit 1 .y: plain LES cells), the Smagorinsky one for the others.
+struct ClosureHook2 {
+  TcPair *sh;
+  uint32_t *phase;
+  float2 wall;
+  uint32_t live;
+  __device__ __forceinline__ float2 operator()(const StepParams &p, float2 tau_s, float2 rho, float2 vx, float2 vy,
+                                               float2 vz, float2 pxx, float2 pyy, float2 pzz, float2 pxy, float2 pxz,
+                                               float2 pyz) const {
+    float xa[kIn], xb[kIn];
+#pragma unroll
+    for (int k = 0; k < kIn; k++) xa[k] = xb[k] = 0.0f;
+    if (live & 1u) {
+      const float st[11] = {tau_s.x, rho.x, vx.x, vy.x, vz.x, pxx.x, pyy.x, pzz.x, pxy.x, pxz.x, pyz.x};
+      cell_inputs(p, st, wall.x, xa);
+    }
+    if (live & 2u) {
+      const float st[11] = {tau_s.y, rho.y, vx.y, vy.y, vz.y, pxx.y, pyy.y, pzz.y, pxy.y, pxz.y, pyz.y};
+      cell_inputs(p, st, wall.y, xb);
+    }
+    const float2 c = block_mlp2(*sh, xa, xb, *phase);
+    float2 tau = tau_s;
+    if (live & 1u) tau.x = p.tau0 + (tau_s.x - p.tau0) * fmaxf(0.0f, 1.0f + c.x);
+    if (live & 2u) tau.y = p.tau0 + (tau_s.y - p.tau0) * fmaxf(0.0f, 1.0f + c.y);
+    return tau;
+  }
+};
+
+// A persistent grid: each block sets up the network image and its TMEM
+// columns once, then walks tiles of 64 x 4 cells of one z-plane, tiles W apart
+// for W blocks.  Plain cells and EQ cells without wall links are stored, as in
+// aa_step_fast; every thread takes part in each tile's network.
+// Eight blocks per SM (64 registers; all 512 TMEM columns): measured 6%
+// faster than six (80 registers) and 9% faster than four.
+#ifndef PW_CLOSURE_PAIR_BLOCKS
+#define PW_CLOSURE_PAIR_BLOCKS 8
+#endif
+static_assert(PW_CLOSURE_PAIR_BLOCKS * 64 <= 512, "the blocks of an SM must fit its 512 TMEM columns");
+template <int ST, int OP, bool ODD>
+__global__ void __launch_bounds__(128, PW_CLOSURE_PAIR_BLOCKS) closure_pairs(StepParams p, const uint32_t *frag, const uint8_t *wall_dist,
+                                                        uint32_t runs, uint32_t row_blocks) {
+  using S = pw::Store<ST>;
+  using T = typename S::T;
+  __shared__ TcPair sh;
+  tc_setup(sh, frag);
+  uint32_t phase = 0;
+  T *f = reinterpret_cast<T *>(p.f);
+  const uint32_t tiles = runs * row_blocks * p.nz;
+  for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const uint32_t run = tile % runs, rest = tile / runs;
+    const uint32_t x = run * 64u + threadIdx.x, y = (rest % row_blocks) * 4u + threadIdx.y, z = rest / row_blocks;
+    const bool row_in = y < p.ny;
+    const uint32_t n = x + p.nx * ((row_in ? y : 0u) + p.ny * z);
+    uint32_t ok = 0u, eq = 0u;
+    if (row_in) {
+#pragma unroll
+      for (uint32_t k = 0; k < 2u; k++) {
+        const uint32_t xk = x + 32u * k, nk = n + 32u * k;
+        if (xk >= p.nx) continue;
+        if (!((__ldg(&p.special[nk >> 5]) >> (nk & 31u)) & 1u)) {
+          if (pwclosure::is_plain_position(xk, p.nx)) ok |= 1u << k;
+        } else if (__ldg(&p.flags[nk]) == pw::EQ) {
+          ok |= 1u << k;
+          eq |= 1u << k;
+        }
+      }
+    }
+    const uint32_t live = ok & ~eq;
+    // odd steps pull across the periodic y and z faces on the seam rows
+    const pwclosure::SeamWrap sw = ODD && row_in ? pwclosure::SeamWrap(p, y, z, 1) : pwclosure::SeamWrap();
+    float2 g[19];
+#pragma unroll
+    for (int i = 0; i < 19; i++) {
+      if (row_in) {
+        const T *a = f + (n + p.ld[i] + sw.of(i));
+        g[i] = make_float2(S::raw(a[0]), S::raw(a[32]));
+      } else {
+        g[i] = make_float2(0.0f, 0.0f);
+      }
+    }
+    float2 eux = pwclosure::f2(p.u_in), euy = pwclosure::f2(0.f), euz = pwclosure::f2(0.f);
+    if (eq) {
+      const uint32_t row = y + p.ny * z;
+      if ((eq & 1u) && x == p.nx - 1 && x > 0) {
+        const float4 u = p.plane_in[row];
+        eux.x = u.x; euy.x = u.y; euz.x = u.z;
+      }
+      if ((eq & 2u) && x + 32u == p.nx - 1) {
+        const float4 u = p.plane_in[row];
+        eux.y = u.x; euy.y = u.y; euz.y = u.z;
+      }
+    }
+    const float2 wall = make_float2((live & 1u) ? (float)wall_dist[n] : 0.0f, (live & 2u) ? (float)wall_dist[n + 32] : 0.0f);
+    float2 rho, vx, vy, vz;
+    const float2 om = pwclosure::update_fast2<OP, true, ClosureHook2>(
+        p, g, rho, vx, vy, vz, S::kScale, S::kInvScale, eq, eux, euy, euz, ClosureHook2{&sh, &phase, wall, live});
+    if (!ok) continue;
+    if (ST != pw::STORE_F32) {
+      // a non-finite state is stored as NaN, as the reference's GPUs store it
+      if (!(fabsf(rho.x + om.x) < INFINITY)) {
+#pragma unroll
+        for (int j = 0; j < 19; j++) g[j].x = __uint_as_float(0x7fc00000u);
+      }
+      if (!(fabsf(rho.y + om.y) < INFINITY)) {
+#pragma unroll
+        for (int j = 0; j < 19; j++) g[j].y = __uint_as_float(0x7fc00000u);
+      }
+    }
+    const uint32_t nk = n * 0x9e3779b9u, nk2 = nk + 32u * 0x9e3779b9u;
+    const uint32_t xa = x, xb = x + 32u;
+#pragma unroll
+    for (int j = 0; j < 19; j++) {
+      // odd steps: the EQ cell at x = 0 pushes c_x = -1 to x = nx - 1 and the
+      // one at x = nx - 1 pushes c_x = +1 to x = 0 (signed element offsets)
+      const int cx = pw::cx_of(j);
+      const int64_t wa = !ODD ? 0 : (cx < 0 && xa == 0u ? (int64_t)p.nx : (cx > 0 && xa + 1u == p.nx ? -(int64_t)p.nx : 0));
+      const int64_t wb = ODD && cx > 0 && xb + 1u == p.nx ? -(int64_t)p.nx : 0;
+      T ca, cb;
+      pwclosure::encode_two<ST>(g[j], j, nk, nk2, ca, cb);
+      T *a = f + (n + p.st[j] + sw.of(pw::opp_of(j)));
+      if (ok & 1u) a[wa] = ca;
+      if (ok & 2u) a[32 + wb] = cb;
+    }
+    if (p.write_macro) {
+      const bool bad_a = (ok & ~eq & 1u) && !(rho.x >= 0.5f && rho.x <= 1.5f);
+      const bool bad_b = (ok & ~eq & 2u) && !(rho.y >= 0.5f && rho.y <= 1.5f);
+      if (bad_a || bad_b) atomicOr(p.status, 1u);
+      if (ok & 1u) p.macros[n] = make_float4(rho.x, vx.x, vy.x, vz.x);
+      if (ok & 2u) p.macros[n + 32] = make_float4(rho.y, vx.y, vy.y, vz.y);
+    }
+    const bool pub_a = (ok & 1u) && x + 2u == p.nx, pub_b = (ok & 2u) && x + 34u == p.nx;
+    if (pub_a || pub_b) {
+      // the outlet's upstream plane publishes the velocity of its stored codes
+      const uint32_t xo = pub_a ? x : x + 32u, no = n + (xo - x);
+      const pwclosure::Nbr b = pwclosure::make_nbr(p, xo, y, z);
+      T code[19];
+#pragma unroll
+      for (int j = 0; j < 19; j++) code[j] = f[pwclosure::slot_of<ODD>(b, j, p.stride, no)];
+      p.plane_out[y + p.ny * z] = pwclosure::outlet_velocity_of<ST>(code);
+    }
   }
   if (threadIdx.x == 0 && threadIdx.y == 0 && sh.failed) atomicOr(p.status, 4u);
   tc_teardown(sh);
@@ -764,6 +1030,65 @@ void launch_closure_step(const StepParams &p, int storage, int op, bool odd, dim
     else PW_CL_LAUNCH(pw::STORE_F32, pw::OP_TRT);
   }
 #undef PW_CL_LAUNCH
+}
+
+template <int ST, int OP, bool ODD>
+static void closure_pairs_step(const StepParams &p, const uint32_t *frag, const uint8_t *wall, const uint32_t *list,
+                               uint32_t count, cudaStream_t s, cudaStream_t t) {
+  // the grid is the blocks that fit at once: the launch bound's count per SM
+  // (registers; 20 KB of shared memory and 64 TMEM columns a block leave room
+  // for more).  No occupancy query: the first step may run under stream capture.
+  static int sms[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) { cudaGetLastError(); dev = 0; }
+  if (!sms[dev] && cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    sms[dev] = 1;
+  }
+  const int blocks_per_sm = PW_CLOSURE_PAIR_BLOCKS;
+  // the floor layer and the wall-link cells beside the plain cells
+  if constexpr (ST != pw::STORE_F32) {
+    if (p.floor_rows && p.ny >= 3u) {
+      const dim3 grid((p.nx + 2 * pwclosure::BX - 1) / (2 * pwclosure::BX), (p.ny - 2u + pwclosure::BY - 1u) / pwclosure::BY);
+      pwclosure::aa_step_floor<ST, OP, true, ODD><<<grid, dim3(pwclosure::BX, pwclosure::BY), 0, t>>>(p);
+    }
+  }
+  if (count)
+    pwclosure::aa_step_edges<ST, OP, true, ODD>
+        <<<(count + pwclosure::NTHREADS - 1) / pwclosure::NTHREADS, pwclosure::NTHREADS, 0, t>>>(p, list, count);
+  const uint32_t runs = (p.nx + 63u) / 64u, row_blocks = (p.ny + 3u) / 4u;
+  const uint32_t tiles = runs * row_blocks * p.nz;
+  const unsigned g = (unsigned)std::min<uint32_t>(tiles, (uint32_t)std::max(blocks_per_sm, 1) * (uint32_t)sms[dev]);
+  closure_pairs<ST, OP, ODD><<<g, dim3(32, 4), 0, s>>>(p, frag, wall, runs, row_blocks);
+}
+
+void launch_closure_pairs(const StepParams &p, int storage, int op, bool odd, const uint32_t *frag,
+                          const uint8_t *wall, const uint32_t *list, uint32_t count, cudaStream_t s,
+                          const pwfast::SideStream *side) {
+  cudaStream_t t = side ? side->stream : s;
+  if (side) {
+    cudaEventRecord(side->fork, s);
+    cudaStreamWaitEvent(t, side->fork, 0);
+  }
+#define PW_CLP(ST, OPV)                                                             \
+  do {                                                                              \
+    if (odd) closure_pairs_step<ST, OPV, true>(p, frag, wall, list, count, s, t);   \
+    else closure_pairs_step<ST, OPV, false>(p, frag, wall, list, count, s, t);      \
+  } while (0)
+  if (op == pw::OP_REG) {
+    if (storage == pw::STORE_F16) PW_CLP(pw::STORE_F16, pw::OP_REG);
+    else if (storage == pw::STORE_BF16) PW_CLP(pw::STORE_BF16, pw::OP_REG);
+    else PW_CLP(pw::STORE_F32, pw::OP_REG);
+  } else {
+    if (storage == pw::STORE_F16) PW_CLP(pw::STORE_F16, pw::OP_TRT);
+    else if (storage == pw::STORE_BF16) PW_CLP(pw::STORE_BF16, pw::OP_TRT);
+    else PW_CLP(pw::STORE_F32, pw::OP_TRT);
+  }
+#undef PW_CLP
+  if (side) {
+    cudaEventRecord(side->join, t);
+    cudaStreamWaitEvent(s, side->join, 0);
+  }
 }
 
 int wall_distance_of(const uint32_t *flags, uint32_t nx, uint32_t ny, uint32_t nz, uint8_t *out, cudaStream_t s) {

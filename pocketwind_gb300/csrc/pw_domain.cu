@@ -286,6 +286,9 @@ void enqueue_step(pw_domain *d, uint64_t step, float u_in, int write_macro) {
                              d->tile_smem, d->stream);
   else if (d->desc.strict)
     pwstrict::launch_step(p, d->desc.storage, d->desc.op, d->desc.les, odd, d->grid, d->stream);
+  else if (d->closure_frag && d->split)
+    pwclosure_host::launch_closure_pairs(p, d->desc.storage, d->desc.op, odd, d->closure_frag, d->wall_dist, d->edges,
+                                         d->edge_own, d->stream, &d->side);
   else if (d->closure_frag)
     pwclosure_host::launch_closure_step(p, d->desc.storage, d->desc.op, odd, d->grid, d->closure_frag, d->wall_dist,
                                         d->stream);
@@ -404,6 +407,11 @@ cudaGraphExec_t graph_for(pw_domain *d, int start_parity, int macro_last) {
 
 // The fast step's edge list and its launch shapes; nblocks becomes the edge
 // kernel's block count (at least 1), within the partial arrays' allocation.
+// Force partial slots of a split step: one per block of the edge kernel.
+size_t edge_blocks(const pw_domain *d) {
+  return d->edge_count ? (d->edge_count + pw::kBlockX * pw::kBlockY - 1) / (pw::kBlockX * pw::kBlockY) : 1;
+}
+
 int build_edge_list(pw_domain *d, Allocs &a) {
   const uint32_t cells = (uint32_t)d->cells;
   const uint32_t nblk = (cells + kEdgeBlock - 1) / kEdgeBlock;
@@ -429,7 +437,7 @@ int build_edge_list(pw_domain *d, Allocs &a) {
   if (e != cudaSuccess) return cuda_status(e, "pw_domain_create edge list");
   d->edge_count = total[0] + total[1];
   d->edge_own = total[0];
-  d->nblocks = d->edge_count ? (d->edge_count + pw::kBlockX * pw::kBlockY - 1) / (pw::kBlockX * pw::kBlockY) : 1;
+  d->nblocks = edge_blocks(d);
   d->plain_grid = d->nx >= 3 ? d->grid : dim3(0, 0, 0);
   return PW_OK;
 }
@@ -864,7 +872,7 @@ int pw_profile_steps(pw_domain *d, uint64_t count, float kernel_ms[3]) {
       const uint64_t step = d->steps + 1;
       pw::StepParams p = params_for(d, step, ramp_speed(d, step), 0);
       const bool odd = (step & 1) != 0;
-      if (d->split) {
+      if (d->split && !d->closure_frag) {
         pwfast::launch_step_split(p, d->desc.storage, d->desc.op, d->desc.les, odd, d->plain_grid, d->edges,
                                   d->edge_own, d->stream, ev[b]);
       } else {
@@ -912,6 +920,7 @@ namespace pwhost {
 MemberView member_view(const pw_domain *d) {
   MemberView v;
   v.split = d->split;
+  v.closure = d->closure_frag != nullptr;
   v.storage = d->desc.storage;
   v.op = d->desc.op;
   v.les = d->desc.les;
@@ -947,13 +956,16 @@ extern "C" int pw_closure_attach(pw_domain *d, const pw_closure *c) {
       if (rc != PW_OK) return rc;
     }
     d->closure_frag = pwclosure_host::fragments(c);
-    d->split = false;
-    d->nblocks = (size_t)d->grid.x * d->grid.y * d->grid.z;
+    // periodic faces: the cell-pair closure step with the edge list beside it
+    // (the split step's partials); free-slip faces: the one-cell closure step
+    // over the cell tiles
+    d->split = d->slip == 0u;
+    d->nblocks = d->split ? edge_blocks(d) : (size_t)d->grid.x * d->grid.y * d->grid.z;
   } else {
     if (!d->closure_frag) return PW_OK;
     d->closure_frag = nullptr;
     d->split = true;
-    d->nblocks = d->edge_count ? (d->edge_count + pw::kBlockX * pw::kBlockY - 1) / (pw::kBlockX * pw::kBlockY) : 1;
+    d->nblocks = edge_blocks(d);
   }
   drop_graphs(d);
   PW_TRY(cudaMemsetAsync(d->partials[0], 0, (size_t)d->grid.x * d->grid.y * d->grid.z * 3 * sizeof(double), d->stream));

@@ -44,6 +44,7 @@ void noalloc_prepare_device();
 // What a batch needs of a member domain (pw_batch.cu).
 struct MemberView {
   bool split;                // fast build, one cell per thread (plain kernels + edge list)
+  bool closure;              // a learned closure is attached
   int storage, op, les;
   uint32_t nx, ny, nz;
   uint64_t steps;

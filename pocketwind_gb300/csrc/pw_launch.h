@@ -62,10 +62,17 @@ PW_DECLARE_LAUNCHERS(pwstrict)
 
 struct pw_closure;
 // The learned closure's step (pw_closure.cu) for a domain with a closure attached:
-// one cell per thread over the tile grid, network inference on the tensor cores.
+// one cell per thread over the tile grid, network inference on the tensor cores
+// (free-slip faces).
 namespace pwclosure_host {
 void launch_closure_step(const pw::StepParams &p, int storage, int op, bool odd, dim3 grid, const uint32_t *frag,
                          const uint8_t *wall, cudaStream_t s);
+// The same step for periodic faces in the cell-pair form: every row's plain
+// cells two per thread with the network on the block's two 128-cell tiles, and
+// the listed edge cells (and the floor layer) beside them on side's stream.
+void launch_closure_pairs(const pw::StepParams &p, int storage, int op, bool odd, const uint32_t *frag,
+                          const uint8_t *wall, const uint32_t *list, uint32_t count, cudaStream_t s,
+                          const pwfast::SideStream *side);
 int wall_distance_of(const uint32_t *flags, uint32_t nx, uint32_t ny, uint32_t nz, uint8_t *out, cudaStream_t s);
 const uint32_t *fragments(const pw_closure *c);
 }

@@ -343,11 +343,20 @@ __device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(__fdividef
 
 // Lanes flagged in eq (bit 0: .x, bit 1: .y) come out at the equilibrium of
 // rho 1 and velocity (eux, euy, euz) instead: their moments are replaced and
-// their relaxation rates set to 1 before the reconstruction.
-template <int OP, bool LES>
+// their relaxation rates set to 1 before the reconstruction.  Hook (LES) maps
+// both lanes' Smagorinsky relaxation time to the one used, as update_fast's
+// hook does for one cell; every thread of a block calls it once.
+struct NoHook2 {
+  __device__ __forceinline__ float2 operator()(const StepParams &, float2 tau_s, float2, float2, float2, float2,
+                                               float2, float2, float2, float2, float2, float2) const {
+    return tau_s;
+  }
+};
+
+template <int OP, bool LES, class Hook = NoHook2>
 __device__ __forceinline__ float2 update_fast2(const StepParams &p, float2 *g, float2 &rho, float2 &vx, float2 &vy,
                                                float2 &vz, const float scale, const float inv_scale, uint32_t eq,
-                                               float2 eux, float2 euy, float2 euz) {
+                                               float2 eux, float2 euy, float2 euz, const Hook &hook = Hook()) {
   float2 s[10], d[10];
 #pragma unroll
   for (int k = 1; k <= 9; k++) {
@@ -390,7 +399,9 @@ __device__ __forceinline__ float2 update_fast2(const StepParams &p, float2 *g, f
       const float t0 = p.tau0;
       const float2 norm = make_float2(q.x > 0.0f ? q.x * rsqrtf(q.x) : 0.0f, q.y > 0.0f ? q.y * rsqrtf(q.y) : 0.0f);
       const float2 arg = fma2(f2(p.cs_term), mul2(norm, inv), f2(t0 * t0));
-      const float2 tau_plus = mul2(f2(0.5f), add2(f2(t0), make_float2(arg.x * rsqrtf(arg.x), arg.y * rsqrtf(arg.y))));
+      const float2 tau_plus =
+          hook(p, mul2(f2(0.5f), add2(f2(t0), make_float2(arg.x * rsqrtf(arg.x), arg.y * rsqrtf(arg.y)))), rho, vx,
+               vy, vz, pxx, pyy, pzz, pxy, pxz, pyz);
       om_p = rcp2(tau_plus);
       om_m = rcp2(fma2(f2(p.lambda), rcp2(sub2(tau_plus, f2(0.5f))), f2(0.5f)));
     }

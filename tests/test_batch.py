@@ -148,6 +148,18 @@ def test_batch_refuses_mixed_or_misused_members():
     with pytest.raises(solver.RangeError):
         batch.step(1)
     batch.destroy()
+    # a member with a learned closure attached steps through the closure's own kernel
+    from pocketwind_gb300.closure import Closure
+    les = [solver.GpuSolver.create(t[k].layout, geometry.voxelize(t[k].body, None, t[k].layout, False),
+                                   solver.SolverParams(tau0=t[k].tau0, u_in=0.05, precision="f16", les=True,
+                                                       operator="reg")) for k in range(2)]
+    net = Closure(1)
+    net.attach(les[0])
+    with pytest.raises(solver.RangeError):
+        Batch(les)
+    Closure.detach(les[0])
+    Batch(les).destroy()
+    net.destroy()
 
 
 @pytest.mark.gpu

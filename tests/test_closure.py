@@ -168,26 +168,27 @@ def test_training_data_match_oracle():
 
 
 @pytest_gpu
-@pytest.mark.parametrize("walls", ["bb", "bouzidi"])
-def test_untrained_closure_is_plain_smagorinsky(walls):
+@pytest.mark.parametrize("walls,lateral", [("bb", "periodic"), ("bouzidi", "periodic"), ("bb", "free-slip")])
+def test_untrained_closure_is_plain_smagorinsky(walls, lateral):
     """An untrained network (c = 0) attached to a domain reproduces plain
     Smagorinsky, with halfway walls and with interpolated (Bouzidi) walls, whose
-    wall values and force the closure kernel takes through the same one-cell
-    path (walls.wgsl:6-21)."""
+    wall cells run in the same edge kernel with or without the closure
+    (walls.wgsl:6-21), and with free-slip faces, where the one-cell closure
+    kernel runs."""
     from pocketwind_gb300 import cases, solver
     from pocketwind_gb300.closure import Closure
     v = cases.vehicle_case(64)
     v.walls = walls
     grid = v.grid()
     mk = lambda: solver.GpuSolver.create(v.layout, grid, solver.SolverParams(tau0=v.tau0, u_in=0.05, les=True,
-                                                                             operator="reg", walls=walls))
+                                                                             operator="reg", walls=walls,
+                                                                             lateral=lateral))
     plain, closed = mk(), mk()
     c = Closure(5)
     c.attach(closed)
-    # The closure kernel evaluates Smagorinsky with the one-cell code path, the
-    # plain domain with the packed two-cell one: they agree to rounding, and this
-    # flow at tau0 = 0.509 amplifies rounding differences about tenfold every
-    # ten steps (measured: 1e-7 at step 10, 1.4e-5 at 30), so the comparison is
+    # With c = 0 the closure's relaxation time tau0 + (tau_s - tau0) can differ
+    # from tau_s in the last bit, and this flow at tau0 = 0.509 amplifies
+    # rounding differences about tenfold every ten steps, so the comparison is
     # made at step 20.
     plain.step(20, True)
     closed.step(20, True)
