@@ -503,6 +503,12 @@ def closure_leg(fine_steps, train_steps, threads, snapshots=8):
     out["fine_cd_re640"] = ref
     out["average_window_flow_throughs"] = 2
     out["coarse_re640"] = coarse
+    # device time of a closure step over a plain Smagorinsky step on the same grid
+    out["closure_kernel"] = ("closure_pairs: the plain step's two-cell update with the network on two 128-cell "
+                             "tcgen05 tiles per block; edge and floor kernels beside it")
+    out["closure_over_plain_step"] = {
+        walls: coarse["closure" + suffix]["ms_per_step"] / coarse["smagorinsky" + suffix]["ms_per_step"]
+        for suffix, walls in (("", "halfway"), ("_bouzidi", "bouzidi"))}
     net.destroy()
     floor_net.destroy()
     return out
