@@ -313,7 +313,10 @@ PW_API int pw_closure_dataset_read(pw_closure *c, uint64_t first, uint64_t count
 PW_API int pw_closure_train(pw_closure *c, uint32_t steps, uint32_t batch, float lr, uint64_t seed,
                             float *loss_first, float *loss_last);
 /* Attach (c) or detach (NULL) a closure to an LES domain of the fast build; the
-   domain restarts from its initial state.  The closure must outlive the attachment. */
+   domain restarts from its initial state.  The closure must outlive the attachment.
+   The closure acts on the plain fluid cells; the wall-link cells keep plain
+   Smagorinsky and the wall model.  A domain with a closure attached cannot join
+   a batch (PW_ERR_INVALID). */
 PW_API int pw_closure_attach(pw_domain *dom, const pw_closure *c);
 
 PW_API int pw_time_steps(pw_domain *dom, uint64_t count, float *ms);
