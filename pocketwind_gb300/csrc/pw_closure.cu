@@ -32,6 +32,7 @@
 #define PW_NS pwclosure
 #define PW_STRICT 0
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include <vector>
 
@@ -587,17 +588,25 @@ __global__ void __launch_bounds__(128, PW_CLOSURE_PAIR_BLOCKS) closure_pairs(Ste
       }
     }
     const uint32_t live = ok & ~eq;
-    // odd steps pull across the periodic y and z faces on the seam rows
-    const pwclosure::SeamWrap sw = ODD && row_in ? pwclosure::SeamWrap(p, y, z, 1) : pwclosure::SeamWrap();
+    // odd steps pull across the periodic y and z faces on the seam rows; a
+    // warp is one row, so the seam rows take their own (warp-uniform) path
+    const bool seam = ODD && row_in && (y == 0u || y + 1u == p.ny || z == 0u || z + 1u == p.nz);
+    const pwclosure::SeamWrap sw = seam ? pwclosure::SeamWrap(p, y, z, 1) : pwclosure::SeamWrap();
     float2 g[19];
+    const auto load = [&](auto wrap) {
 #pragma unroll
-    for (int i = 0; i < 19; i++) {
-      if (row_in) {
-        const T *a = f + (n + p.ld[i] + sw.of(i));
+      for (int i = 0; i < 19; i++) {
+        const T *a = f + (n + p.ld[i] + (decltype(wrap)::value ? sw.of(i) : 0));
         g[i] = make_float2(S::raw(a[0]), S::raw(a[32]));
-      } else {
-        g[i] = make_float2(0.0f, 0.0f);
       }
+    };
+    if (!row_in) {
+#pragma unroll
+      for (int i = 0; i < 19; i++) g[i] = make_float2(0.0f, 0.0f);
+    } else if (seam) {
+      load(std::true_type());
+    } else {
+      load(std::false_type());
     }
     float2 eux = pwclosure::f2(p.u_in), euy = pwclosure::f2(0.f), euz = pwclosure::f2(0.f);
     if (eq) {
@@ -629,19 +638,31 @@ __global__ void __launch_bounds__(128, PW_CLOSURE_PAIR_BLOCKS) closure_pairs(Ste
     }
     const uint32_t nk = n * 0x9e3779b9u, nk2 = nk + 32u * 0x9e3779b9u;
     const uint32_t xa = x, xb = x + 32u;
+    const auto store = [&](auto wrap) {
 #pragma unroll
-    for (int j = 0; j < 19; j++) {
-      // odd steps: the EQ cell at x = 0 pushes c_x = -1 to x = nx - 1 and the
-      // one at x = nx - 1 pushes c_x = +1 to x = 0 (signed element offsets)
-      const int cx = pw::cx_of(j);
-      const int64_t wa = !ODD ? 0 : (cx < 0 && xa == 0u ? (int64_t)p.nx : (cx > 0 && xa + 1u == p.nx ? -(int64_t)p.nx : 0));
-      const int64_t wb = ODD && cx > 0 && xb + 1u == p.nx ? -(int64_t)p.nx : 0;
-      T ca, cb;
-      pwclosure::encode_two<ST>(g[j], j, nk, nk2, ca, cb);
-      T *a = f + (n + p.st[j] + sw.of(pw::opp_of(j)));
-      if (ok & 1u) a[wa] = ca;
-      if (ok & 2u) a[32 + wb] = cb;
-    }
+      for (int j = 0; j < 19; j++) {
+        // odd steps: the EQ cell at x = 0 pushes c_x = -1 to x = nx - 1 and the
+        // one at x = nx - 1 pushes c_x = +1 to x = 0 (signed element offsets)
+        int64_t wa = 0, wb = 0, ws = 0;
+        if constexpr (decltype(wrap)::value) {
+          const int cx = pw::cx_of(j);
+          wa = cx < 0 && xa == 0u ? (int64_t)p.nx : (cx > 0 && xa + 1u == p.nx ? -(int64_t)p.nx : 0);
+          wb = cx > 0 && xb + 1u == p.nx ? -(int64_t)p.nx : 0;
+          ws = sw.of(pw::opp_of(j));
+        }
+        T ca, cb;
+        pwclosure::encode_two<ST>(g[j], j, nk, nk2, ca, cb);
+        T *a = f + (n + p.st[j] + ws);
+        if (ok & 1u) a[wa] = ca;
+        if (ok & 2u) a[32 + wb] = cb;
+      }
+    };
+    // the wrapping stores for the seam rows and for warps with an EQ cell at
+    // either x face on odd steps
+    if (ODD && (seam || __any_sync(__activemask(), (ok & eq) && (x == 0u || x + 33u >= p.nx))))
+      store(std::true_type());
+    else
+      store(std::false_type());
     if (p.write_macro) {
       const bool bad_a = (ok & ~eq & 1u) && !(rho.x >= 0.5f && rho.x <= 1.5f);
       const bool bad_b = (ok & ~eq & 2u) && !(rho.y >= 0.5f && rho.y <= 1.5f);
