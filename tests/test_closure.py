@@ -204,6 +204,33 @@ def test_untrained_closure_is_plain_smagorinsky(walls, lateral):
 
 
 @pytest_gpu
+@pytest.mark.parametrize("precision", ["f16", "bf16"])
+def test_untrained_closure_16bit_within_storage_noise(precision):
+    """With 16-bit storage the closure's kernel pairs cells x and x + 32 of a
+    row, the plain step's cell-pair kernel x and x + 1, so the two round each
+    code with another dither realization (same probabilities); the floor
+    layer runs in the floor kernel beside both.  An untrained network then
+    stays within the storage's rounding noise of plain Smagorinsky: after 40
+    steps of the 64x32x32 vehicle, velocity within relative L2 2e-3 (f16) and
+    1e-2 (bf16), the tolerances of the floor kernel's own check."""
+    from pocketwind_gb300 import cases, solver
+    from pocketwind_gb300.closure import Closure
+    v = cases.vehicle_case(64)
+    grid = v.grid()
+    mk = lambda: solver.GpuSolver.create(v.layout, grid, solver.SolverParams(tau0=v.tau0, u_in=0.05, les=True,
+                                                                             operator="reg", precision=precision))
+    plain, closed = mk(), mk()
+    c = Closure(5)
+    c.attach(closed)
+    plain.step(40, True)
+    closed.step(40, True)
+    ua, ub = closed.macros()[:, 1:].astype(np.float64), plain.macros()[:, 1:].astype(np.float64)
+    assert np.isfinite(ua).all()
+    assert np.linalg.norm(ua - ub) / np.linalg.norm(ub) < (2e-3 if precision == "f16" else 1e-2)
+    c.destroy()
+
+
+@pytest_gpu
 def test_trained_closure_beats_smagorinsky_on_held_out_data():
     """What the network gains over the method without it: after training on
     filtered fine-grid samples its a-priori error on held-out samples is below
