@@ -139,7 +139,9 @@ struct TcShared {
 
 // Bounded wait on the MMA barrier's phase `parity`; false when it ran out
 // (the caller then skips the network and keeps plain Smagorinsky, c = 0).
-__device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity) {
+// Before returning false it waits once more, also bounded, so that an MMA
+// still in flight can finish before its operands or columns are reused.
+__device__ __forceinline__ bool tc_wait_once(uint64_t *bar, uint32_t parity) {
   for (uint32_t it = 0; it < (1u << 22); it++) {
     uint32_t ok;
     asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -148,6 +150,11 @@ __device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity) {
                  : "memory");
     if (ok) return true;
   }
+  return false;
+}
+__device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity) {
+  if (tc_wait_once(bar, parity)) return true;
+  tc_wait_once(bar, parity);
   return false;
 }
 
@@ -418,9 +425,9 @@ __global__ void __launch_bounds__(128, 4) closure_step(StepParams p, const uint3
 // model, as in a step without the closure.
 struct TcPair {
   __align__(128) unsigned char img[kImgBytes];   // the network image
-  // the layer-2 operands of the two tiles (128 x 32 bf16 each); the layer-1
-  // operands (128 x 16) share their first half, which layer 1's MMAs have
-  // read by the time its outputs come back
+  // the layer-2 operands of the two tiles (128 x 32 bf16 each); the two
+  // layer-1 operands (128 x 16 each) share the first tile's, which layer 1's
+  // MMAs have read by the time their outputs come back
   __align__(128) unsigned char a2[2][128 * 64];
   __align__(8) uint64_t bar;                     // MMA completion
   uint32_t tmem;                                 // 64 TMEM columns: tile t's layer output at column 32 t
