@@ -166,8 +166,15 @@ class GpuSolver:
         return ForceSample(s.step, s.fx, s.fy, s.fz)
 
     # -------------------------------------------------------------- fields
-    def macros(self) -> np.ndarray:
-        out = np.empty((self.cells, 4), np.float32)
+    def macros(self, out: np.ndarray = None) -> np.ndarray:
+        """(rho, ux, uy, uz) per cell (macroBuffer, docs/numerics.md:147-155), into `out` when
+        given: a C-contiguous float32 array of shape (cells, 4) that the caller keeps from
+        one readout to the next."""
+        if out is None:
+            out = np.empty((self.cells, 4), np.float32)
+        elif (not isinstance(out, np.ndarray) or out.dtype != np.float32 or out.shape != (self.cells, 4)
+              or not out.flags.c_contiguous or not out.flags.writeable):
+            raise RangeError("out must be a writeable C-contiguous float32 array of shape (cells, 4).")
         _lib.check(_lib.load().pw_read_macros(self._live(), out.ctypes.data_as(C.c_void_p)), "macros")
         return out
 

@@ -287,6 +287,13 @@ def test_write_read_round_trip_and_totals():
         assert abs(t[0] - g[:, live].sum()) < 1e-9
         for a in range(3):
             assert abs(t[1 + a] - (C[:, a][:, None] * g[:, live]).sum()) < 1e-9
+        # the macros into a caller's buffer equal the ones into a fresh array
+        buf = np.full((CELLS, 4), np.nan, np.float32)
+        assert gpu.macros(out=buf) is buf and np.array_equal(buf, gpu.macros())
+        for bad in (np.empty((CELLS, 4), np.float64), np.empty((CELLS, 3), np.float32),
+                    np.empty((4, CELLS), np.float32).T):
+            with pytest.raises(ValueError):
+                gpu.macros(out=bad)
 
 
 def test_ramp_matches_reference_schedule():
