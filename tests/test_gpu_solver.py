@@ -461,6 +461,30 @@ def test_free_slip_fast_matches_fp64_reference(op, les):
         assert norm_err(gpu.macros()[:, 1:].astype(np.float64), cpu.macros()[:, 1:]) < 1e-5, cp
 
 
+@pytest.mark.parametrize("precision,op,les", [("f16", "trt", False), ("f16", "reg", True), ("bf16", "trt", False),
+                                               ("f32", "trt", False)])
+def test_fast_step_is_deterministic(precision, op, les):
+    """The fast build's step gives the same stored codes every time: its
+    kernels run concurrently on two streams, and no cell's result may depend
+    on their timing (an inflow or outflow cell's loads outside its row, which
+    other cells rewrite during the step, once leaked into its equilibrium
+    through rounding).  Four runs of the same voxelized sphere with EQ faces,
+    60 steps each, are bit for bit equal."""
+    from pocketwind_gb300 import meshes
+    G, S = _pw()
+    layout = (64, 32, 32)
+    grid = G.voxelize(meshes.icosphere((16, 16, 16), 5, 3), None, layout, False)
+    runs = []
+    for _ in range(4):
+        s = S.GpuSolver.create(layout, grid, S.SolverParams(tau0=0.56, u_in=0.05, les=les, operator=op,
+                                                            precision=precision))
+        s.step(60, True)
+        runs.append(s.populations_raw().view(np.uint8).copy())
+        s.destroy()
+    for r in runs[1:]:
+        assert np.array_equal(r, runs[0])
+
+
 def test_free_slip_write_read_round_trip_and_mass():
     """Write-in and readout follow the reflected slots in both layouts; a closed
     free-slip channel conserves mass."""
