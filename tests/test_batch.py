@@ -195,3 +195,24 @@ def test_floor_kernel_matches_the_general_path(precision):
     fa, fb = alone.read_force(), member.read_force()
     assert abs(fa.fx - fb.fx) <= tol * abs(fb.fx)
     batch.destroy()
+
+
+@pytest.mark.gpu
+def test_batch_step_is_deterministic():
+    """A batch's two concurrent launches give the same stored codes every
+    time: two batches of the same three tunnels, 60 steps each, are bit for
+    bit equal member by member."""
+    from pocketwind_gb300.batch import Batch
+    tunnels = cases.batch_tunnels(3, 7)
+    runs = []
+    for _ in range(2):
+        members = [_make(t, "f16") for t in tunnels]
+        batch = Batch(members)
+        batch.step(60, True)
+        runs.append([m.populations_raw().view(np.uint8).copy() for m in members])
+        batch.destroy()
+        for m in members:
+            m.destroy()
+    for a, b in zip(runs[0], runs[1]):
+        assert np.array_equal(a, b)
+

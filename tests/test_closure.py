@@ -231,6 +231,27 @@ def test_untrained_closure_16bit_within_storage_noise(precision):
 
 
 @pytest_gpu
+def test_closure_step_is_deterministic():
+    """With a network whose output is not zero, two runs of the closure step
+    (the tensor-core kernel with the edge and floor kernels beside it) give the
+    same stored codes bit for bit after 40 steps."""
+    from pocketwind_gb300 import cases, solver
+    v = cases.vehicle_case(64)
+    grid = v.grid()
+    net = _closure(_rand_params(9))
+    runs = []
+    for _ in range(2):
+        s = solver.GpuSolver.create(v.layout, grid, solver.SolverParams(tau0=v.tau0, u_in=0.05, les=True,
+                                                                         operator="reg", precision="f16"))
+        net.attach(s)
+        s.step(40, True)
+        runs.append(s.populations_raw().view(np.uint8).copy())
+        s.destroy()
+    net.destroy()
+    assert np.array_equal(runs[0], runs[1])
+
+
+@pytest_gpu
 def test_trained_closure_beats_smagorinsky_on_held_out_data():
     """What the network gains over the method without it: after training on
     filtered fine-grid samples its a-priori error on held-out samples is below
