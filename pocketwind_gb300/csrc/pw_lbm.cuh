@@ -342,11 +342,12 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __
 __device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(__fdividef(1.0f, a.x), __fdividef(1.0f, a.y)); }
 
 // Lanes flagged in eq (bit 0: .x, bit 1: .y) come out at the equilibrium of
-// rho 1 and velocity (eux, euy, euz) instead: their loaded values are zeroed
-// (on odd steps an x-face EQ cell's c_x = +-1 loads fall outside its row, on
-// slots that another EQ cell may be writing in the same step, and TRT's
-// s - (s - 2 e) would carry their rounding into the result), their moments
-// replaced and their relaxation rates set to 1 before the reconstruction.  Hook (LES) maps
+// rho 1 and velocity (eux, euy, euz) instead: their moments are replaced and
+// their relaxation rates set to 1 before the reconstruction.  For TRT their
+// loaded values are zeroed first: on odd steps an x-face EQ cell's c_x = +-1
+// loads fall outside its row, on slots that another EQ cell may be writing in
+// the same step, and TRT's s - (s - 2 e) would carry their rounding into the
+// result (REG multiplies them by an exact zero).  Hook (LES) maps
 // both lanes' Smagorinsky relaxation time to the one used, as update_fast's
 // hook does for one cell; every thread of a block calls it once.
 struct NoHook2 {
@@ -360,11 +361,13 @@ template <int OP, bool LES, class Hook = NoHook2>
 __device__ __forceinline__ float2 update_fast2(const StepParams &p, float2 *g, float2 &rho, float2 &vx, float2 &vy,
                                                float2 &vz, const float scale, const float inv_scale, uint32_t eq,
                                                float2 eux, float2 euy, float2 euz, const Hook &hook = Hook()) {
-  if (eq) {
+  if constexpr (OP == OP_TRT) {
+    if (eq) {
 #pragma unroll
-    for (int i = 0; i < 19; i++) {
-      if (eq & 1u) g[i].x = 0.0f;
-      if (eq & 2u) g[i].y = 0.0f;
+      for (int i = 0; i < 19; i++) {
+        if (eq & 1u) g[i].x = 0.0f;
+        if (eq & 2u) g[i].y = 0.0f;
+      }
     }
   }
   float2 s[10], d[10];
