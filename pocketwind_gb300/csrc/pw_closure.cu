@@ -1017,10 +1017,8 @@ int refresh_fragments(pw_closure *c) {
 }  // namespace
 
 namespace pwclosure_host {
-// The closure step for a domain with an attached closure (pw_domain.cu).
-void launch_closure_step(const StepParams &p, int storage, int op, bool odd, dim3 grid, const uint32_t *frag,
-                         const uint8_t *wall, cudaStream_t s) {
-  const dim3 blk(32, 4);
+// Multiprocessors of the current device, cached per device (1 when unknown).
+static int sm_count() {
   static int sms[64] = {};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) { cudaGetLastError(); dev = 0; }
@@ -1028,8 +1026,15 @@ void launch_closure_step(const StepParams &p, int storage, int op, bool odd, dim
     cudaGetLastError();
     sms[dev] = 1;
   }
+  return std::max(sms[dev], 1);
+}
+
+// The closure step for a domain with an attached closure (pw_domain.cu).
+void launch_closure_step(const StepParams &p, int storage, int op, bool odd, dim3 grid, const uint32_t *frag,
+                         const uint8_t *wall, cudaStream_t s) {
+  const dim3 blk(32, 4);
   const uint32_t tiles = grid.x * grid.y * grid.z;
-  const unsigned g = (unsigned)std::min<uint32_t>(tiles, 4u * (uint32_t)std::max(sms[dev], 1));
+  const unsigned g = (unsigned)std::min<uint32_t>(tiles, 4u * (uint32_t)sm_count());
 #define PW_CL_LAUNCH(ST, OPV)                                                                  \
   do {                                                                                        \
     if (odd) closure_step<ST, OPV, true><<<g, blk, 0, s>>>(p, frag, wall, grid.x, grid.y);    \
@@ -1053,13 +1058,6 @@ static void closure_pairs_step(const StepParams &p, const uint32_t *frag, const 
   // the grid is the blocks that fit at once: the launch bound's count per SM
   // (registers; 20 KB of shared memory and 64 TMEM columns a block leave room
   // for more).  No occupancy query: the first step may run under stream capture.
-  static int sms[64] = {};
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) { cudaGetLastError(); dev = 0; }
-  if (!sms[dev] && cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
-    cudaGetLastError();
-    sms[dev] = 1;
-  }
   const int blocks_per_sm = PW_CLOSURE_PAIR_BLOCKS;
   // the floor layer and the wall-link cells beside the plain cells
   if constexpr (ST != pw::STORE_F32) {
@@ -1073,7 +1071,7 @@ static void closure_pairs_step(const StepParams &p, const uint32_t *frag, const 
         <<<(count + pwclosure::NTHREADS - 1) / pwclosure::NTHREADS, pwclosure::NTHREADS, 0, t>>>(p, list, count);
   const uint32_t runs = (p.nx + 63u) / 64u, row_blocks = (p.ny + 3u) / 4u;
   const uint32_t tiles = runs * row_blocks * p.nz;
-  const unsigned g = (unsigned)std::min<uint32_t>(tiles, (uint32_t)std::max(blocks_per_sm, 1) * (uint32_t)sms[dev]);
+  const unsigned g = (unsigned)std::min<uint32_t>(tiles, (uint32_t)blocks_per_sm * (uint32_t)sm_count());
   closure_pairs<ST, OP, ODD><<<g, dim3(32, 4), 0, s>>>(p, frag, wall, runs, row_blocks);
 }
 
